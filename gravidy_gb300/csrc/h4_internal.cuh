@@ -1,0 +1,103 @@
+// Internal device-side layout and kernel entry points of the Hermite4 block
+// step.  Host code (h4_capi.cu) owns the allocations; kernels get the arrays
+// through H4Dev, passed by value.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace h4 {
+
+// 32-byte aligned double4: one 256-bit access per element on sm_100+.
+typedef double4_32a dbl4;
+__host__ __device__ __forceinline__ dbl4 make_dbl4(double x, double y, double z, double w) {
+    dbl4 r;
+    r.x = x; r.y = y; r.z = z; r.w = w;
+    return r;
+}
+
+// Per-system control block in device memory.  Every block-time quantity of a
+// step lives here, so a step can run without the host reading anything back.
+struct H4Ctrl {
+    double itime;                  // current block time (ITIME)
+    unsigned long long atime_bits; // next block time (ATIME), as the bit
+                                   // pattern of a non-negative double, so
+                                   // atomicMin on it is a min on the value
+    unsigned int nact;             // active particles of the current step
+    unsigned int work_next;        // work-queue head of the force kernel
+    unsigned int work_total;       // work items of the current force launch
+    unsigned int force_split;      // j-chunks per active group (S)
+    unsigned int n_blocks_flag;    // blocks of the active-set kernels
+    unsigned int err;              // sticky error bits (H4_ERRBIT_*)
+    // h4_advance bookkeeping
+    double t_stop;                 // stop when itime >= t_stop
+    double t_log;                  // stop when itime >= t_log
+    unsigned long long steps;      // block steps done
+    unsigned long long psteps;     // sum of nact
+    unsigned long long inter;      // sum of nact * n
+    unsigned long long max_steps;  // hard bound on steps of one advance call
+    int running;                   // 1 while the device loop continues
+    int pad_;
+};
+
+enum : unsigned int {
+    H4_ERRBIT_NONFINITE = 1u,      // non-finite value met in the corrector
+    H4_ERRBIT_SPLIT = 2u,          // partial-force scratch too small
+    H4_ERRBIT_STEPCAP = 4u,        // device loop reached its step bound
+};
+
+struct H4Dev {
+    int n;          // particles
+    int n_pad;      // predicted arrays are padded to a multiple of 256
+    double e2;      // softening squared
+    double eta;     // timestep parameter (float value held in double)
+    double dt_min, dt_max;
+    dbl4 *r, *v;         // corrected position (w = mass) and velocity
+    double *f, *old;        // [6n] acc/jerk, Forces layout (a[3], a1[3])
+    double *a2, *a3;        // [3n] double3 layout
+    double *t, *dt;         // [n]
+    dbl4 *pr, *pv;       // [n_pad] predicted position (w = mass), velocity
+    unsigned int *move;     // [n] active list
+    unsigned int *blk_cnt;  // [n_blocks_flag] active count per chunk
+    double *part;           // partial forces, [S][6][nact] for the current step
+    size_t part_cap;        // capacity of part in doubles
+    double *epot_i;         // [n] per-particle potential (energy kernel)
+    double *energy_out;     // [2] kinetic, potential
+    H4Ctrl *ctrl;
+};
+
+constexpr int FLAG_THREADS = 256;
+constexpr int FLAG_ITEMS = 8;                       // elements per thread
+constexpr int FLAG_CHUNK = FLAG_THREADS * FLAG_ITEMS;
+
+// ---- exact-order kernels (h4_step_kernels.cu) ------------------------------
+void launch_find_active(const H4Dev &d, bool host_itime, double itime, cudaStream_t s);
+void launch_save_old(const H4Dev &d, cudaStream_t s);
+void launch_predict(const H4Dev &d, bool host_itime, double itime, cudaStream_t s);
+void launch_reduce_forces(const H4Dev &d, bool save_old, cudaStream_t s);
+void launch_correct(const H4Dev &d, bool host_itime, double itime, bool fused_reduce, cudaStream_t s);
+void launch_next_time(const H4Dev &d, bool reset, cudaStream_t s);
+void launch_init_dt(const H4Dev &d, float eta, double itime, cudaStream_t s);
+void launch_advance_bookkeeping(const H4Dev &d, cudaGraphConditionalHandle cond, bool use_cond,
+                                cudaStream_t s);
+void launch_identity_move(const H4Dev &d, cudaStream_t s);
+void launch_set_nact(const H4Dev &d, unsigned nact, cudaStream_t s);
+void launch_set_atime(const H4Dev &d, double atime, cudaStream_t s);
+void launch_reduce_to(const H4Dev &d, double *out, cudaStream_t s);
+void launch_set_pred_from_state(const H4Dev &d, cudaStream_t s);
+void launch_pad_predicted(const H4Dev &d, cudaStream_t s);
+int kernels_per_step();
+
+// ---- force kernels -----------------------------------------------------------
+// Active list and count come from d.move / d.ctrl->nact; results are written
+// as partial sums into d.part (reduced by launch_reduce_forces/correct).
+void launch_force_fp64(const H4Dev &d, int grid_warps, cudaStream_t s);
+void launch_force_exact(const H4Dev &d, cudaStream_t s);   // writes d.part with S = 1
+int force_fp64_grid_warps(int num_sms);
+
+// ---- energy (h4_energy.cu) --------------------------------------------------
+void launch_energy(const H4Dev &d, cudaStream_t s);
+
+// ---- peaks -------------------------------------------------------------------
+cudaError_t probe_peaks(double *fp64, double *fp32);
+
+}  // namespace h4

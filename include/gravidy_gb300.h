@@ -1,0 +1,176 @@
+/* gravidy_gb300.h -- C ABI of the GB300 (sm_103a) Hermite4 block-step path.
+ *
+ * Drop-in boundary for the GPU backend of GraviDy: the class Hermite4GPU
+ * (src/include/gpu/Hermite4GPU.cuh:100-144) and the Hermite4 base methods it
+ * inherits (src/include/Hermite4.hpp:60-63).  The reference keeps the
+ * particle state in host arrays of NbodySystem (src/include/NbodySystem.hpp:
+ * 98-134) and copies them to and from the device around every kernel; here
+ * the state lives in device memory for the lifetime of a handle and is copied
+ * to the host only on request (h4_download) -- for logs and snapshots.
+ *
+ * Conventions
+ *  - Every call returns an h4_status (0 = success).  Nothing exits or aborts
+ *    the process (the reference's CSC macro calls exit(EXIT_FAILURE),
+ *    Hermite4GPU.cuh:43-50).  h4_last_error() gives a message for the last
+ *    failure on the calling thread.
+ *  - A handle is not thread safe; calls on one handle must be serialised.
+ *  - Host arrays use the reference layouts: h4_double4 is CUDA's double4
+ *    (x, y, z, w; w = mass for positions), h4_forces is the reference's Forces
+ *    (a[3], a1[3]; common.hpp:227-231), h4_double3 is double3.
+ *  - All work is issued on the handle's stream (h4_set_stream); calls that
+ *    return host values synchronise that stream.
+ */
+#ifndef GRAVIDY_GB300_H
+#define GRAVIDY_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define H4_ABI_VERSION 1
+
+typedef struct { double x, y, z, w; } h4_double4;
+typedef struct { double x, y, z; } h4_double3;
+typedef struct { double a[3]; double a1[3]; } h4_forces;
+
+typedef enum {
+    H4_OK = 0,
+    H4_ERR_ARG = 1,        /* invalid argument (null pointer, size, range) */
+    H4_ERR_CUDA = 2,       /* CUDA runtime error; see h4_last_error() */
+    H4_ERR_ALLOC = 3,      /* device or host allocation failed */
+    H4_ERR_STATE = 4,      /* call out of order (e.g. step before init) */
+    H4_ERR_NONFINITE = 5,  /* non-finite value found in the state */
+    H4_ERR_UNSUPPORTED = 6 /* feature not available for this handle */
+} h4_status;
+
+/* Arithmetic of the O(N_act N) force sum. */
+typedef enum {
+    H4_FORCE_FP64 = 0,   /* FP64 pair arithmetic, j-split + fixed-order sums */
+    H4_FORCE_EXACT = 1,  /* FP64 in the reference's exact operation order:
+                            bit-identical forces to the reference CPU path
+                            (slow; a validation mode) */
+    H4_FORCE_MIXED = 2   /* FP32 pair arithmetic, double-single position
+                            deltas, compensated FP32 partial sums, FP64
+                            per-particle reduction */
+} h4_force_mode;
+
+typedef struct h4_system_s *h4_handle;
+
+/* Message of the last failure on this thread ("" if none). */
+const char *h4_last_error(void);
+const char *h4_status_string(int status);
+int h4_abi_version(void);
+
+/* Creation.  Replaces Hermite4GPU::Hermite4GPU + alloc_arrays_device
+ * (Hermite4GPU.cu:40-165) and Hermite4::init_data (Hermite4.cpp:194-240).
+ *   n      number of particles (n >= 1)
+ *   e2     softening squared, as NbodySystem::e2 (NbodySystem.cpp:50)
+ *   eta    timestep accuracy parameter, NbodySystem::eta (-e flag)
+ *   r, v   host arrays of n double4 (r.w = mass, rounded to float as the
+ *          reference does; v.w ignored)
+ *   mode   an h4_force_mode
+ * The state starts as init_data leaves it: predictors = (r, v, m), forces,
+ * timesteps and times zero. */
+int h4_create(h4_handle *out, unsigned int n, double e2, float eta,
+              const h4_double4 *r, const h4_double4 *v, int mode);
+int h4_destroy(h4_handle h);
+
+/* Run the handle's work on a caller-provided stream (cudaStream_t passed as
+ * void*; NULL selects the handle's own non-blocking stream, so the legacy
+ * default stream cannot be selected). */
+int h4_set_stream(h4_handle h, void *stream);
+/* Timestep bounds, D_TIME_MIN / D_TIME_MAX of common.hpp:122,129 (defaults
+ * 2^-23 and 2^-3).  Both must be powers of two with dt_min <= dt_max. */
+int h4_set_dt_limits(h4_handle h, double dt_min, double dt_max);
+int h4_set_force_mode(h4_handle h, int mode);
+
+/* Hermite4GPU::init_acc_jrk (Hermite4GPU.cu:333-375): acc and jerk of all
+ * particles from the current predictors (O(N^2)). */
+int h4_init_acc_jrk(h4_handle h);
+
+/* Hermite4::init_dt (Hermite4.cpp:108-140): Aarseth initial block timesteps
+ * with accuracy parameter eta (the reference passes ETA_S), t = itime for all
+ * particles; *atime = min(*atime, min dt) as the reference's CTIME. */
+int h4_init_dt(h4_handle h, double *atime, float eta, double itime);
+
+/* Hermite4::find_particles_to_move (Hermite4.cpp:63-84): the active set
+ * {i : |itime - (t_i + dt_i)| < 2 DBL_EPSILON} in ascending i, kept on the
+ * device; *nact receives its size. */
+int h4_find_particles_to_move(h4_handle h, double itime, unsigned int *nact);
+
+/* Hermite4::save_old_acc_jrk (Hermite4.cpp:145-153). */
+int h4_save_old_acc_jrk(h4_handle h, unsigned int nact);
+
+/* Hermite4GPU::predicted_pos_vel (Hermite4GPU.cu:201-268): third-order
+ * Taylor prediction of all particles to itime. */
+int h4_predicted_pos_vel(h4_handle h, double itime);
+
+/* Hermite4GPU::update_acc_jrk (Hermite4GPU.cu:385-535): new acc and jerk of
+ * the nact active particles against all N. */
+int h4_update_acc_jrk(h4_handle h, unsigned int nact);
+
+/* Hermite4GPU::correction_pos_vel (Hermite4GPU.cu:274-328, restating
+ * Hermite4CPU.cpp:370-411): Hermite corrector, t = itime, and the new block
+ * timestep (NbodyUtils::get_timestep_normal + normalize_dt,
+ * NbodyUtils.cpp:337-424) of the active particles. */
+int h4_correction_pos_vel(h4_handle h, double itime, unsigned int nact);
+
+/* Hermite4::next_integration_time (Hermite4.cpp:90-102). */
+int h4_next_integration_time(h4_handle h, double *atime);
+
+/* Hermite4GPU::get_energy_gpu (Hermite4GPU.cu:540-592): kinetic and
+ * unsoftened potential energy of the corrected state; returns the total in
+ * *etot (any output pointer may be NULL). */
+int h4_get_energy(h4_handle h, double *ekin, double *epot, double *etot);
+
+/* One whole block step on the device (the loop body of
+ * Hermite4GPU_integration.cpp:81-99): itime = *atime, find active set, save
+ * old forces, predict, force, correct, next time.  Outputs may be NULL;
+ * a non-NULL nact/itime/atime synchronises the stream. */
+int h4_step(h4_handle h, double *atime, double *itime, unsigned int *nact);
+
+/* Advance with device-resident block steps until the block time reaches
+ * t_stop (the reference's "while (ITIME < integration_time)" loop) or a step
+ * reaches t_log (the energy log condition ITIME >= interval * k).  The step
+ * sequence is replayed from a CUDA graph; the host waits once at the end.
+ * *atime is the next block time in and out; the counters accumulate.
+ *   stats[0] = block steps done   stats[1] = particle steps (sum of nact)
+ *   stats[2] = interactions (sum of nact * N)   stats[3] = last itime
+ *   stats[4] = nact of the last step */
+int h4_advance(h4_handle h, double t_stop, double t_log, double *atime,
+               double *itime, double stats[5]);
+
+/* Copy the state to host arrays (any pointer may be NULL; n elements each;
+ * move receives the current active list, entries past nact undefined). */
+int h4_download(h4_handle h, h4_double4 *r, h4_double4 *v, h4_forces *f,
+                h4_forces *old, h4_double3 *a2, h4_double3 *a3, double *t,
+                double *dt, unsigned int *move);
+/* Replace parts of the state (any pointer may be NULL). */
+int h4_upload(h4_handle h, const h4_double4 *r, const h4_double4 *v,
+              const h4_forces *f, const h4_forces *old, const double *t,
+              const double *dt);
+/* Predicted positions/velocities (Predictor array of the reference,
+ * common.hpp:213-218, as two double4 arrays; pr.w = mass). */
+int h4_download_predicted(h4_handle h, h4_double4 *pr, h4_double4 *pv);
+
+/* Stateless force sum for tests and tools: acc/jerk of the particles
+ * listed in move[0..nact) against all n, from predictors (pr.w = mass). */
+int h4_forces_for(h4_handle h, const h4_double4 *pr, const h4_double4 *pv,
+                  unsigned int nact, const unsigned int *move, h4_forces *out);
+
+/* Device time (ms) of the last force kernel launch and of the last
+ * h4_advance call, measured with CUDA events on the handle's stream. */
+int h4_last_timings(h4_handle h, float *force_ms, float *advance_ms);
+/* Kernels launched by this handle since creation. */
+int h4_kernel_launches(h4_handle h, unsigned long long *count);
+
+/* Throughput of the FP64 and FP32 pipes on this GPU (flop/s, FMA = 2),
+ * measured with a short dependent-FMA kernel; used as roofline peaks. */
+int h4_probe_peaks(double *fp64_flops, double *fp32_flops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GRAVIDY_GB300_H */
