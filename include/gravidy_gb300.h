@@ -160,6 +160,34 @@ int h4_download_predicted(h4_handle h, h4_double4 *pr, h4_double4 *pv);
 int h4_forces_for(h4_handle h, const h4_double4 *pr, const h4_double4 *pv,
                   unsigned int nact, const unsigned int *move, h4_forces *out);
 
+/* Force sum that allocates nothing.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc -- an application that hands all
+ * of the GPU's memory to its own pool at start-up, or a time-critical loop
+ * that cannot take the synchronisation an allocation may imply.  Same result
+ * as h4_forces_for (FP64 kernel, same split and summation order), but every
+ * buffer is the caller's device memory and no handle is needed:
+ *   d_pr, d_pv  n predicted positions (w = mass) and velocities, 32-byte
+ *               aligned device arrays of h4_double4
+ *   d_move      nact particle indices (device), d_out nact h4_forces (device)
+ *   stream      cudaStream_t as void* (NULL = the legacy default stream)
+ * The partial sums use a fixed file-scope device array of
+ * H4_NOALLOC_SCRATCH_DOUBLES doubles (16 MiB), held on every GPU that loads
+ * this library until the process exits; nact above H4_NOALLOC_MAX_NACT is
+ * rejected with H4_ERR_ARG.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * The call is asynchronous on `stream`; the message of a failure is
+ * returned by h4_forces_noalloc_error(). */
+#define H4_NOALLOC_SCRATCH_DOUBLES (2u * 1024u * 1024u)
+#define H4_NOALLOC_MAX_NACT (H4_NOALLOC_SCRATCH_DOUBLES / 6u)
+int h4_forces_noalloc(unsigned int n, double e2, const h4_double4 *d_pr,
+                      const h4_double4 *d_pv, unsigned int nact,
+                      const unsigned int *d_move, h4_forces *d_out,
+                      void *stream);
+const char *h4_forces_noalloc_error(void);
+
 /* Device time (ms) of the last force kernel launch and of the last
  * h4_advance call, measured with CUDA events on the handle's stream. */
 int h4_last_timings(h4_handle h, float *force_ms, float *advance_ms);
