@@ -61,6 +61,7 @@ struct h4_system_s {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_mode = -1;
+    unsigned mixed_threshold = MIXED_TILED_THRESHOLD_DEFAULT;
     cudaStream_t graph_stream = nullptr;
 };
 
@@ -68,7 +69,7 @@ namespace {
 
 void free_device(h4_system_s *h) {
     H4Dev &d = h->d;
-    void *ptrs[] = {d.r, d.v, d.f, d.old, d.a2, d.a3, d.t, d.dt, d.pr, d.pv,
+    void *ptrs[] = {d.r, d.v, d.f, d.old, d.a2, d.a3, d.t, d.dt, d.pr, d.pv, d.jf0, d.jf1, d.jf2,
                     d.move, d.blk_cnt, d.part, d.epot_i, d.energy_out, d.ctrl};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -87,13 +88,15 @@ void free_device(h4_system_s *h) {
 int grid_warps(const h4_system_s *h) { return force_fp64_grid_warps(h->num_sms); }
 
 // Force sum of the active list on the device (nact in the control block),
-// leaving partial sums in d.part.
-void launch_force(h4_system_s *h, cudaStream_t s) {
+// leaving partial sums in d.part.  known_nact < 0: count only on the device.
+void launch_force(h4_system_s *h, cudaStream_t s, long long known_nact = -1) {
     switch (h->mode) {
-    case H4_FORCE_EXACT: launch_force_exact(h->d, s); break;
-    default: launch_force_fp64(h->d, grid_warps(h), s); break;
+    case H4_FORCE_EXACT: launch_force_exact(h->d, s); h->launches += 1; break;
+    case H4_FORCE_MIXED:
+        h->launches += launch_force_mixed(h->d, h->num_sms, h->mixed_threshold, known_nact, s);
+        break;
+    default: launch_force_fp64(h->d, grid_warps(h), s); h->launches += 1; break;
     }
-    h->launches += 1;
 }
 
 int check_launch(const char *what) {
@@ -125,6 +128,9 @@ void enqueue_step(h4_system_s *h, cudaStream_t s) {
     launch_next_time(h->d, false, s);
     h->launches += 5;   // find (2 kernels) + predict + correct + next time
 }
+
+// Kernels in one captured block step (force kernels counted per mode).
+int step_kernel_count(const h4_system_s *h) { return 5 + (h->mode == H4_FORCE_MIXED ? 2 : 1); }
 
 int build_graph(h4_system_s *h) {
     if (h->graph_exec && h->graph_mode == h->mode) return H4_OK;
@@ -187,7 +193,6 @@ int h4_create(h4_handle *out, unsigned int n, double e2, float eta, const h4_dou
     if (!(e2 >= 0.0) || !std::isfinite(e2)) return fail(H4_ERR_ARG, "h4_create: e2 must be finite and >= 0");
     if (!(eta > 0.0f) || !std::isfinite(eta)) return fail(H4_ERR_ARG, "h4_create: eta must be > 0");
     if (mode < H4_FORCE_FP64 || mode > H4_FORCE_MIXED) return fail(H4_ERR_ARG, "h4_create: unknown force mode");
-    if (mode == H4_FORCE_MIXED) return fail(H4_ERR_UNSUPPORTED, "h4_create: mixed mode not built");
     for (unsigned i = 0; i < n; i++) {
         if (!std::isfinite(r[i].x) || !std::isfinite(r[i].y) || !std::isfinite(r[i].z) ||
             !std::isfinite(r[i].w) || !std::isfinite(v[i].x) || !std::isfinite(v[i].y) ||
@@ -217,6 +222,8 @@ int h4_create(h4_handle *out, unsigned int n, double e2, float eta, const h4_dou
         {(void **)&d.a2, N * 3 * sizeof(double)}, {(void **)&d.a3, N * 3 * sizeof(double)},
         {(void **)&d.t, N * sizeof(double)},     {(void **)&d.dt, N * sizeof(double)},
         {(void **)&d.pr, NP * sizeof(dbl4)},     {(void **)&d.pv, NP * sizeof(dbl4)},
+        {(void **)&d.jf0, NP * sizeof(float4)},  {(void **)&d.jf1, NP * sizeof(float4)},
+        {(void **)&d.jf2, NP * sizeof(float4)},
         {(void **)&d.move, N * sizeof(unsigned)}, {(void **)&d.blk_cnt, (size_t)nflag * sizeof(unsigned)},
         {(void **)&d.part, d.part_cap * sizeof(double)}, {(void **)&d.epot_i, N * sizeof(double)},
         {(void **)&d.energy_out, 2 * sizeof(double)}, {(void **)&d.ctrl, sizeof(H4Ctrl)},
@@ -295,8 +302,15 @@ int h4_set_dt_limits(h4_handle h, double dt_min, double dt_max) {
 int h4_set_force_mode(h4_handle h, int mode) {
     if (!h) return fail(H4_ERR_ARG, "null handle");
     if (mode < H4_FORCE_FP64 || mode > H4_FORCE_MIXED) return fail(H4_ERR_ARG, "unknown force mode");
-    if (mode == H4_FORCE_MIXED) return fail(H4_ERR_UNSUPPORTED, "mixed mode not built");
     h->mode = mode;
+    return H4_OK;
+}
+
+int h4_set_mixed_threshold(h4_handle h, unsigned int nact_threshold) {
+    if (!h) return fail(H4_ERR_ARG, "null handle");
+    if (nact_threshold < 1) return fail(H4_ERR_ARG, "threshold must be >= 1");
+    h->mixed_threshold = nact_threshold;
+    if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; h->graph_mode = -1; }
     return H4_OK;
 }
 
@@ -309,7 +323,7 @@ int h4_init_acc_jrk(h4_handle h) {
     launch_identity_move(h->d, s);
     h->launches += 1;
     cudaEventRecord(h->ev0, s);
-    launch_force(h, s);
+    launch_force(h, s, (long long)h->d.n);
     cudaEventRecord(h->ev1, s);
     launch_reduce_forces(h->d, false, s);
     h->launches += 2;
@@ -378,7 +392,7 @@ int h4_update_acc_jrk(h4_handle h, unsigned int nact) {
     if (st) return st;
     if (nact == 0) return H4_OK;
     cudaEventRecord(h->ev0, h->stream);
-    launch_force(h, h->stream);
+    launch_force(h, h->stream, (long long)nact);
     cudaEventRecord(h->ev1, h->stream);
     launch_reduce_forces(h->d, false, h->stream);
     h->launches += 1;
@@ -467,7 +481,7 @@ int h4_advance(h4_handle h, double t_stop, double t_log, double *atime, double *
     if ((st = sync_ctrl(h))) return st;
     cudaEventElapsedTime(&h->last_advance_ms, h->ev2, h->ev3);
     const H4Ctrl &o = *h->h_ctrl;
-    h->launches += (unsigned long long)o.steps * (unsigned long long)(kernels_per_step() + 1);
+    h->launches += (unsigned long long)o.steps * (unsigned long long)(step_kernel_count(h) + 1);
     if (atime) *atime = bits_to_double_host(o.atime_bits);
     if (itime) *itime = o.itime;
     if (stats) {
@@ -479,6 +493,7 @@ int h4_advance(h4_handle h, double t_stop, double t_log, double *atime, double *
     }
     if (o.err & H4_ERRBIT_NONFINITE) return fail(H4_ERR_NONFINITE, "h4_advance: non-finite state");
     if (o.err & H4_ERRBIT_STEPCAP) return fail(H4_ERR_STATE, "h4_advance: step bound reached");
+    if (o.err & H4_ERRBIT_TIMEOUT) return fail(H4_ERR_CUDA, "h4_advance: a bounded device wait timed out");
     return H4_OK;
 }
 
@@ -540,7 +555,7 @@ int h4_forces_for(h4_handle h, const h4_double4 *pr, const h4_double4 *pv, unsig
     int st = set_nact(h, nact);
     if (st) return st;
     cudaEventRecord(h->ev0, s);
-    launch_force(h, s);
+    launch_force(h, s, (long long)nact);
     cudaEventRecord(h->ev1, s);
     if ((st = check_launch("h4_forces_for"))) return st;
     if ((st = sync_ctrl(h))) return st;

@@ -1,0 +1,379 @@
+// Mixed-precision acc+jerk force sum (H4_FORCE_MIXED).
+//
+// Same quantity as Hermite4CPU::force_calculation (src/include/cpu/
+// Hermite4CPU.cpp:55-82) summed as in Hermite4GPU::update_acc_jrk
+// (src/include/gpu/Hermite4GPU.cu:385-535), with the arithmetic split by need:
+//  * positions are held as double-single pairs (hi + lo floats); the
+//    difference rj - ri is taken on both parts before it is rounded to float,
+//    so close pairs keep their separation to ~2^-48 of |r|;
+//  * everything else of the pair (r^2, 1/sqrt, A = m/r^3, the jerk term) is
+//    FP32 on the FP32 pipe, 64x the FP64 pipe's rate on GB300;
+//  * each particle's terms are summed in FP32 over sub-tiles of 64 j, and the
+//    sub-tile sums are added into Kahan-compensated FP32 accumulators; the
+//    compensated sum of each j-chunk is stored as a double and the chunks are
+//    added in FP64, in chunk order, by the reduction/corrector kernel.
+// The j data come from three float4 arrays written by the predictor:
+//   jf0 = (x_hi, y_hi, z_hi, m), jf1 = (x_lo, y_lo, z_lo, 0), jf2 = (vx, vy, vz, 0)
+// padded to a multiple of 256 with zero-mass particles (exact zero terms).
+//
+// Two shapes, chosen per launch from the active count:
+//  * tiled: a block owns 512 active particles (4 per thread, lanes over i)
+//    and one j-chunk; the chunk streams through shared memory in tiles of 256
+//    j, each tile brought in by three TMA bulk copies (cp.async.bulk) that
+//    complete on an mbarrier, double buffered;
+//  * warp items (small active sets): a warp owns up to 4 active particles and
+//    one j-chunk, its lanes take interleaved j straight from L2, and the lane
+//    sums are combined with a shuffle tree in FP64.
+// Every wait on an mbarrier is bounded; on timeout the block records
+// H4_ERRBIT_TIMEOUT in the control block and leaves.
+#include <stdint.h>
+
+#include "h4_internal.cuh"
+
+namespace h4 {
+namespace {
+
+constexpr int MT = 128;                 // threads per block (tiled shape)
+constexpr int IPT = 4;                  // active particles per thread
+constexpr int TI = MT * IPT;            // active particles per tile item
+constexpr int JT = 256;                 // j per shared-memory tile
+constexpr int SUB = 64;                 // j per FP32 partial sum
+constexpr int WARPS_W = 4;              // warps per block (warp-item shape)
+constexpr int IGW = 4;                  // active particles per warp item
+constexpr unsigned WAIT_LIMIT = 1u << 26;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// 1-D bulk copy global -> shared, completion counted on `bar` (16-byte
+// aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+struct IParticle {
+    float xh, yh, zh, xl, yl, zl, vx, vy, vz;
+};
+
+__device__ __forceinline__ IParticle load_i(const H4Dev &d, unsigned i) {
+    const float4 a = d.jf0[i], b = d.jf1[i], c = d.jf2[i];
+    IParticle p;
+    p.xh = a.x; p.yh = a.y; p.zh = a.z;
+    p.xl = b.x; p.yl = b.y; p.zl = b.z;
+    p.vx = c.x; p.vy = c.y; p.vz = c.z;
+    return p;
+}
+
+// One pair, FP32 after the double-single difference.  `sum` gets the six
+// terms (acc, jerk).  With e2 = 0 the self term is masked explicitly; with
+// e2 > 0 it is an exact zero (dr = dv = 0).
+template <bool MASK_SELF>
+__device__ __forceinline__ void pair_mixed(const IParticle &p, float4 j0, float4 j1, float4 j2, float e2,
+                                           bool self, float sum[6]) {
+    const float dx = (j0.x - p.xh) + (j1.x - p.xl);
+    const float dy = (j0.y - p.yh) + (j1.y - p.yl);
+    const float dz = (j0.z - p.zh) + (j1.z - p.zl);
+    const float dvx = j2.x - p.vx, dvy = j2.y - p.vy, dvz = j2.z - p.vz;
+    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e2)));
+    float m = j0.w;
+    if (MASK_SELF) {
+        r2 = self ? 1.0f : r2;
+        m = self ? 0.0f : m;
+    }
+    const float rinv = rsqrtf(r2);
+    const float r2inv = rinv * rinv;
+    const float A = (m * rinv) * r2inv;
+    const float rv = fmaf(dx, dvx, fmaf(dy, dvy, dz * dvz));
+    const float eta = rv * (-3.0f * r2inv);
+    sum[0] = fmaf(A, dx, sum[0]);
+    sum[1] = fmaf(A, dy, sum[1]);
+    sum[2] = fmaf(A, dz, sum[2]);
+    sum[3] = fmaf(A, fmaf(eta, dx, dvx), sum[3]);
+    sum[4] = fmaf(A, fmaf(eta, dy, dvy), sum[4]);
+    sum[5] = fmaf(A, fmaf(eta, dz, dvz), sum[5]);
+}
+
+struct MixedSplit {
+    unsigned split, total, n_groups;
+    int chunk;
+};
+
+// j-split of the tiled shape: chunks are whole tiles of the padded arrays.
+__device__ __forceinline__ MixedSplit tiled_split(const H4Dev &d, unsigned nact, unsigned blocks) {
+    MixedSplit s;
+    s.n_groups = (nact + TI - 1) / TI;
+    unsigned split = (blocks * 6 + s.n_groups - 1) / s.n_groups;
+    const unsigned tiles = (unsigned)(d.n_pad / JT);
+    if (split > tiles) split = tiles;
+    const unsigned cap = (unsigned)(d.part_cap / (6ull * nact));
+    if (split > cap) split = cap;
+    if (split < 1) split = 1;
+    const unsigned tiles_per_chunk = (tiles + split - 1) / split;
+    s.chunk = (int)(tiles_per_chunk * JT);
+    s.split = (unsigned)((d.n_pad + s.chunk - 1) / s.chunk);
+    s.total = s.n_groups * s.split;
+    return s;
+}
+
+template <bool MASK_SELF>
+__global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled(H4Dev d, unsigned threshold) {
+    __shared__ __align__(128) float4 sj[2][3][JT];
+    __shared__ __align__(8) uint64_t full[2];
+    __shared__ unsigned s_item;
+    const unsigned nact = d.ctrl->nact;
+    if (nact == 0 || nact < threshold) return;   // the warp-item kernel takes small sets
+    const MixedSplit sp = tiled_split(d, nact, gridDim.x);
+    const int tid = threadIdx.x;
+    if (blockIdx.x == 0 && tid == 0) {
+        d.ctrl->force_split = sp.split;
+        d.ctrl->work_total = sp.total;
+    }
+    if (tid == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const float e2 = (float)d.e2;
+    unsigned gt = 0;   // tiles consumed by this block so far (buffer = gt & 1, parity = (gt >> 1) & 1)
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(&d.ctrl->work_next, 1u);
+        __syncthreads();
+        const unsigned item = s_item;
+        __syncthreads();
+        if (item >= sp.total) break;
+        const unsigned s = item / sp.n_groups;
+        const unsigned g = item - s * sp.n_groups;
+        const int j_begin = (int)s * sp.chunk;
+        const int j_end = min(d.n_pad, j_begin + sp.chunk);
+        const int ntiles = (j_end - j_begin) / JT;
+
+        IParticle ip[IPT];
+        unsigned idx[IPT];
+        float S[IPT][6], C[IPT][6];
+#pragma unroll
+        for (int q = 0; q < IPT; q++) {
+            const unsigned k = g * TI + tid + q * MT;
+            idx[q] = d.move[k < nact ? k : nact - 1];
+            ip[q] = load_i(d, idx[q]);
+#pragma unroll
+            for (int c = 0; c < 6; c++) { S[q][c] = 0.f; C[q][c] = 0.f; }
+        }
+        // prefetch the first two tiles
+        if (tid == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            for (int t = 0; t < 2 && t < ntiles; t++) {
+                const unsigned b = (gt + t) & 1u;
+                const size_t j0 = (size_t)j_begin + (size_t)t * JT;
+                mbar_arrive_expect_tx(&full[b], 3 * JT * sizeof(float4));
+                tma_load_1d(&sj[b][0][0], d.jf0 + j0, JT * sizeof(float4), &full[b]);
+                tma_load_1d(&sj[b][1][0], d.jf1 + j0, JT * sizeof(float4), &full[b]);
+                tma_load_1d(&sj[b][2][0], d.jf2 + j0, JT * sizeof(float4), &full[b]);
+            }
+        }
+        for (int t = 0; t < ntiles; t++, gt++) {
+            const unsigned b = gt & 1u, parity = (gt >> 1) & 1u;
+            unsigned spins = 0;
+            bool ok = true;
+            while (!mbar_try_wait(&full[b], parity)) {
+                if (++spins > WAIT_LIMIT) { ok = false; break; }
+            }
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_TIMEOUT);
+                return;
+            }
+            const int jt0 = j_begin + t * JT;
+#pragma unroll 1
+            for (int sb = 0; sb < JT; sb += SUB) {
+                float part[IPT][6];
+#pragma unroll
+                for (int q = 0; q < IPT; q++)
+#pragma unroll
+                    for (int c = 0; c < 6; c++) part[q][c] = 0.f;
+#pragma unroll 4
+                for (int jj = sb; jj < sb + SUB; jj++) {
+                    const float4 j0 = sj[b][0][jj], j1 = sj[b][1][jj], j2 = sj[b][2][jj];
+#pragma unroll
+                    for (int q = 0; q < IPT; q++)
+                        pair_mixed<MASK_SELF>(ip[q], j0, j1, j2, e2, (unsigned)(jt0 + jj) == idx[q], part[q]);
+                }
+#pragma unroll
+                for (int q = 0; q < IPT; q++)
+#pragma unroll
+                    for (int c = 0; c < 6; c++) kahan_add(S[q][c], C[q][c], part[q][c]);
+            }
+            __syncthreads();   // every thread is done with buffer b
+            if (tid == 0 && t + 2 < ntiles) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const size_t j0 = (size_t)j_begin + (size_t)(t + 2) * JT;
+                mbar_arrive_expect_tx(&full[b], 3 * JT * sizeof(float4));
+                tma_load_1d(&sj[b][0][0], d.jf0 + j0, JT * sizeof(float4), &full[b]);
+                tma_load_1d(&sj[b][1][0], d.jf1 + j0, JT * sizeof(float4), &full[b]);
+                tma_load_1d(&sj[b][2][0], d.jf2 + j0, JT * sizeof(float4), &full[b]);
+            }
+        }
+        double *p = d.part + (size_t)s * 6 * nact;
+#pragma unroll
+        for (int q = 0; q < IPT; q++) {
+            const unsigned k = g * TI + tid + q * MT;
+            if (k < nact) {
+#pragma unroll
+                for (int c = 0; c < 6; c++) p[(size_t)c * nact + k] = (double)S[q][c] - (double)C[q][c];
+            }
+        }
+    }
+}
+
+// ---- warp items: small active sets --------------------------------------------
+__device__ __forceinline__ MixedSplit warp_split(const H4Dev &d, unsigned nact, unsigned total_warps) {
+    MixedSplit s;
+    s.n_groups = (nact + IGW - 1) / IGW;
+    unsigned split = (total_warps * 8 + s.n_groups - 1) / s.n_groups;
+    const unsigned max_split = (unsigned)((d.n + 127) / 128);
+    if (split > max_split) split = max_split;
+    const unsigned cap = (unsigned)(d.part_cap / (6ull * nact));
+    if (split > cap) split = cap;
+    if (split < 1) split = 1;
+    int chunk = (d.n + (int)split - 1) / (int)split;
+    chunk = (chunk + 31) & ~31;
+    s.chunk = chunk;
+    s.split = (unsigned)((d.n + chunk - 1) / chunk);
+    s.total = s.n_groups * s.split;
+    return s;
+}
+
+template <int NI, bool MASK_SELF>
+__device__ __forceinline__ void warp_item(const H4Dev &d, unsigned nact, unsigned k0, int j_begin, int j_end,
+                                          unsigned s, int lane, float e2) {
+    IParticle ip[NI];
+    unsigned idx[NI];
+    float S[NI][6], C[NI][6];
+#pragma unroll
+    for (int q = 0; q < NI; q++) {
+        idx[q] = d.move[k0 + q];
+        ip[q] = load_i(d, idx[q]);
+#pragma unroll
+        for (int c = 0; c < 6; c++) { S[q][c] = 0.f; C[q][c] = 0.f; }
+    }
+    for (int jb = j_begin; jb < j_end; jb += 32 * 16) {
+        float part[NI][6];
+#pragma unroll
+        for (int q = 0; q < NI; q++)
+#pragma unroll
+            for (int c = 0; c < 6; c++) part[q][c] = 0.f;
+        const int jl = min(j_end, jb + 32 * 16);
+        for (int j = jb + lane; j < jl; j += 32) {
+            const float4 j0 = d.jf0[j], j1 = d.jf1[j], j2 = d.jf2[j];
+#pragma unroll
+            for (int q = 0; q < NI; q++) pair_mixed<MASK_SELF>(ip[q], j0, j1, j2, e2, (unsigned)j == idx[q], part[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < NI; q++)
+#pragma unroll
+            for (int c = 0; c < 6; c++) kahan_add(S[q][c], C[q][c], part[q][c]);
+    }
+#pragma unroll
+    for (int q = 0; q < NI; q++) {
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            double a = (double)S[q][c] - (double)C[q][c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            if (lane == 0) d.part[(size_t)s * 6 * nact + (size_t)c * nact + k0 + q] = a;
+        }
+    }
+}
+
+template <bool MASK_SELF>
+__global__ void __launch_bounds__(WARPS_W * 32) k_force_mixed_warp(H4Dev d, unsigned threshold) {
+    const unsigned nact = d.ctrl->nact;
+    if (nact == 0 || nact >= threshold) return;   // the tiled kernel takes large sets
+    const int lane = threadIdx.x & 31;
+    const MixedSplit sp = warp_split(d, nact, gridDim.x * WARPS_W);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        d.ctrl->force_split = sp.split;
+        d.ctrl->work_total = sp.total;
+    }
+    const float e2 = (float)d.e2;
+    for (;;) {
+        unsigned item;
+        if (lane == 0) item = atomicAdd(&d.ctrl->work_next, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= sp.total) break;
+        const unsigned s = item / sp.n_groups;
+        const unsigned g = item - s * sp.n_groups;
+        const int j_begin = (int)s * sp.chunk;
+        const int j_end = min(d.n, j_begin + sp.chunk);
+        const unsigned k0 = g * IGW;
+        const unsigned cnt = min((unsigned)IGW, nact - k0);
+        if (cnt == 4) {
+            warp_item<4, MASK_SELF>(d, nact, k0, j_begin, j_end, s, lane, e2);
+        } else {
+            unsigned k = k0;
+            if (cnt >= 2) { warp_item<2, MASK_SELF>(d, nact, k, j_begin, j_end, s, lane, e2); k += 2; }
+            if (cnt & 1) warp_item<1, MASK_SELF>(d, nact, k, j_begin, j_end, s, lane, e2);
+        }
+    }
+}
+
+}  // namespace
+
+// Both shapes are launched when the active count is only known on the device
+// (the captured block step); the one not chosen returns at once.  When the
+// host knows the count (known_nact >= 0) only the chosen one is launched.
+int launch_force_mixed(const H4Dev &d, int num_sms, unsigned threshold, long long known_nact, cudaStream_t s) {
+    const bool mask = !(d.e2 > 0.0);
+    int launched = 0;
+    const bool want_tiled = known_nact < 0 || (unsigned long long)known_nact >= threshold;
+    const bool want_warp = known_nact < 0 || (unsigned long long)known_nact < threshold;
+    if (want_tiled) {
+        if (mask)
+            k_force_mixed_tiled<true><<<num_sms * 3, MT, 0, s>>>(d, threshold);
+        else
+            k_force_mixed_tiled<false><<<num_sms * 3, MT, 0, s>>>(d, threshold);
+        launched++;
+    }
+    if (want_warp) {
+        if (mask)
+            k_force_mixed_warp<true><<<num_sms * 4, WARPS_W * 32, 0, s>>>(d, threshold);
+        else
+            k_force_mixed_warp<false><<<num_sms * 4, WARPS_W * 32, 0, s>>>(d, threshold);
+        launched++;
+    }
+    return launched;
+}
+
+}  // namespace h4

@@ -43,6 +43,7 @@ enum : unsigned int {
     H4_ERRBIT_NONFINITE = 1u,      // non-finite value met in the corrector
     H4_ERRBIT_SPLIT = 2u,          // partial-force scratch too small
     H4_ERRBIT_STEPCAP = 4u,        // device loop reached its step bound
+    H4_ERRBIT_TIMEOUT = 8u,        // a bounded wait (mbarrier) gave up
 };
 
 struct H4Dev {
@@ -56,6 +57,8 @@ struct H4Dev {
     double *a2, *a3;        // [3n] double3 layout
     double *t, *dt;         // [n]
     dbl4 *pr, *pv;       // [n_pad] predicted position (w = mass), velocity
+    float4 *jf0, *jf1, *jf2; // [n_pad] predicted j data for the mixed kernels:
+                             // (x_hi, y_hi, z_hi, m), (x_lo, y_lo, z_lo, 0), (vx, vy, vz, 0)
     unsigned int *move;     // [n] active list
     unsigned int *blk_cnt;  // [n_blocks_flag] active count per chunk
     double *part;           // partial forces, [S][6][nact] for the current step
@@ -92,6 +95,9 @@ int kernels_per_step();
 // as partial sums into d.part (reduced by launch_reduce_forces/correct).
 void launch_force_fp64(const H4Dev &d, int grid_warps, cudaStream_t s);
 void launch_force_exact(const H4Dev &d, cudaStream_t s);   // writes d.part with S = 1
+// Returns the number of kernels launched (1 or 2).
+int launch_force_mixed(const H4Dev &d, int num_sms, unsigned threshold, long long known_nact, cudaStream_t s);
+constexpr unsigned MIXED_TILED_THRESHOLD_DEFAULT = 4096;
 int force_fp64_grid_warps(int num_sms);
 
 // ---- energy (h4_energy.cu) --------------------------------------------------

@@ -84,6 +84,26 @@ __device__ unsigned block_sum(unsigned x) {
     return s;
 }
 
+// Double-single split of a double: hi = fl32(x), lo = fl32(x - hi).
+__device__ __forceinline__ void ds_split(double x, float &hi, float &lo) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(__dadd_rn(x, -(double)hi));
+}
+
+// Packed FP32 j data of the mixed kernels, from predicted position/velocity.
+__device__ __forceinline__ void write_jf(const H4Dev &d, int i, const dbl4 &pr, const dbl4 &pv) {
+    float4 a, b, c;
+    ds_split(pr.x, a.x, b.x);
+    ds_split(pr.y, a.y, b.y);
+    ds_split(pr.z, a.z, b.z);
+    a.w = (float)pr.w;
+    b.w = 0.f;
+    c = make_float4((float)pv.x, (float)pv.y, (float)pv.z, 0.f);
+    d.jf0[i] = a;
+    d.jf1[i] = b;
+    d.jf2[i] = c;
+}
+
 // ---- active set (Hermite4::find_particles_to_move) --------------------------
 // Pass 1: active count of each chunk of FLAG_CHUNK particles.
 __global__ void __launch_bounds__(FLAG_THREADS)
@@ -167,6 +187,7 @@ __global__ void __launch_bounds__(256) k_predict(H4Dev d, int host_itime, double
     pv.w = 0.0;
     d.pr[i] = pr;
     d.pv[i] = pv;
+    if (d.jf0) write_jf(d, i, pr, pv);
 }
 
 // Predictors straight from the state (Hermite4::init_data, Hermite4.cpp:
@@ -179,6 +200,7 @@ __global__ void k_pred_from_state(H4Dev d) {
     v.w = 0.0;
     d.pr[i] = r;
     d.pv[i] = v;
+    if (d.jf0) write_jf(d, i, r, v);
 }
 
 // Padding of the predicted arrays past n: zero mass, far away, at rest.
@@ -189,6 +211,11 @@ __global__ void k_pad_predicted(H4Dev d) {
     if (i >= d.n_pad) return;
     d.pr[i] = make_dbl4(1.0e15, 1.0e15, 1.0e15, 0.0);
     d.pv[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);
+    if (d.jf0) {
+        d.jf0[i] = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 0.f);
+        d.jf1[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        d.jf2[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
 }
 
 __global__ void k_identity_move(H4Dev d) {

@@ -246,6 +246,13 @@ class Hermite4GPU:
                                         mv.ctypes.data, out.ctypes.data))
         return out
 
+    def set_mixed_threshold(self, nact_threshold: int):
+        _lib.check(self.L.h4_set_mixed_threshold(self.h, int(nact_threshold)))
+
+    def set_force_mode(self, mode: str):
+        _lib.check(self.L.h4_set_force_mode(self.h, _lib.MODES[mode]))
+        self.mode = mode
+
     def last_timings(self):
         f, a = C.c_float(), C.c_float()
         _lib.check(self.L.h4_last_timings(self.h, C.byref(f), C.byref(a)))

@@ -1,0 +1,96 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports
+every declared symbol, argument validation, the input format, the energy log
+format, and the initial-condition generators."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from gravidy_gb300 import _lib, ics
+from gravidy_gb300.hermite4 import e2_from_softening
+from gravidy_gb300.io import EnergyLog, read_input_file
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    text = open(os.path.join(ROOT, "include", "gravidy_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(h4_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.load()
+    syms = _declared_symbols()
+    assert len(syms) >= 25
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+    assert set(syms) == set(_lib.SIGNATURES), set(syms) ^ set(_lib.SIGNATURES)
+    assert L.h4_abi_version() == 1
+
+
+def test_create_validates_arguments_before_touching_the_device():
+    L = _lib.load()
+    h = C.c_void_p()
+    r = np.zeros((4, 4)); v = np.zeros((4, 4))
+    assert L.h4_create(C.byref(h), 0, 1e-4, C.c_float(0.01), r.ctypes.data, v.ctypes.data, 0) == 1
+    assert L.h4_create(C.byref(h), 4, -1.0, C.c_float(0.01), r.ctypes.data, v.ctypes.data, 0) == 1
+    assert L.h4_create(C.byref(h), 4, 1e-4, C.c_float(0.01), None, v.ctypes.data, 0) == 1
+    assert L.h4_create(C.byref(h), 4, 1e-4, C.c_float(0.01), r.ctypes.data, v.ctypes.data, 7) == 1
+    r[2, 1] = np.nan
+    assert L.h4_create(C.byref(h), 4, 1e-4, C.c_float(0.01), r.ctypes.data, v.ctypes.data, 0) == 5
+    assert b"particle 2" in L.h4_last_error()
+    assert L.h4_destroy(None) == 0
+    assert L.h4_step(None, None, None, None) == 1
+
+
+def test_e2_is_the_float_product():
+    assert e2_from_softening(0.01) == float(np.float32(np.float32(0.01) * np.float32(0.01)))
+    assert e2_from_softening(1e-4) != 1e-8
+
+
+def test_reader_rounds_mass_to_float_and_stops_at_bad_line(tmp_path):
+    p = tmp_path / "in.txt"
+    p.write_text("# Time: 0.25\n# comment\n0 0.1 1 2 3 4 5 6\n1 0.3 1e-3 2 3 4 5 6\n2 0.5 1 2 3\n3 0.1 1 1 1 1 1 1\n")
+    d = read_input_file(str(p))
+    assert d.n == 2 and d.snapshot_time == 0.25
+    assert d.mass[0] == float(np.float32(0.1)) and d.mass[1] == float(np.float32(0.3))
+    assert d.pos[1, 0] == 1e-3 and d.warnings
+
+
+def test_reader_drops_last_line_without_newline(tmp_path):
+    p = tmp_path / "in.txt"
+    p.write_text("0 0.5 1 2 3 4 5 6\n1 0.5 1 2 3 4 5 6")
+    assert read_input_file(str(p)).n == 1
+
+
+def test_energy_log_format():
+    log = EnergyLog(stream=False)
+    head = log.row(0.0, 0, 0, -0.25, 0.1).splitlines()
+    assert head[0].split() == ["#", "IteTime", "Iter", "Nsteps", "Energy", "RelE", "CumE", "ElapsedTime", "GFLOPS"]
+    row = log.row(0.125, 486, 28942, -0.25003355903, 0.48, 100, 1.0).split()
+    assert row[:4] == ["00", "0.125", "486", "28942"]
+    assert row[4] == "-2.5003355903e-01" and row[6] == "1.342361e-04"
+
+
+@pytest.mark.parametrize("imf", ["equal", "salpeter"])
+def test_plummer_henon_units(imf):
+    m, p, v = ics.plummer(2000, 5, imf)
+    assert abs(m.sum() - 1.0) < 1e-6
+    assert np.all(m == m.astype(np.float32))
+    k, u = ics.energy(p, v, m)
+    assert abs(k + u + 0.25) < 1e-12 and abs(2 * k + u) < 1e-12
+    assert np.abs((m[:, None] * p).sum(0)).max() < 1e-12
+    if imf == "salpeter":
+        mm = m / m.min()
+        assert mm.max() > 50   # spans the [0.1, 100] range after normalisation
+
+
+def test_plummer_is_seeded():
+    a = ics.plummer(500, 9)
+    b = ics.plummer(500, 9)
+    c = ics.plummer(500, 10)
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    assert not np.array_equal(a[1], c[1])
