@@ -1,0 +1,121 @@
+#include "OptionsParser.hpp"
+
+#include <sys/stat.h>
+
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <sstream>
+
+namespace gb300 {
+
+OptionsParser::OptionsParser(int argc, char *argv[])
+    : integration_time(1.0f), interval_time((float)D_TIME_MAX), gpus(0), snapshot_time(0.0f),
+      softening((float)E), eta(ETA_N), snapshot_number(0), length_output_number(0), resume(false),
+      force_mode(H4_FORCE_FP64), host_steps(false), argc_(argc), argv_(argv) {
+    ops.print_screen = false;
+    ops.print_all = false;
+    ops.print_lagrange = false;
+}
+
+bool OptionsParser::file_exists(const std::string &filename) const {
+    struct stat buffer;
+    return stat(filename.c_str(), &buffer) != -1;
+}
+
+std::string OptionsParser::usage() const {
+    std::ostringstream s;
+    s << "GraviDy (GB300)\n"
+      << "  -h [ --help ]                  Display this message\n"
+      << "Required options:\n"
+      << "  -i [ --input ] <filename>      Input data filename\n"
+      << "  -t [ --time ] <value> (=1)     Integration time (In N-body units)\n"
+      << "Elective options:\n"
+      << "  -o [ --output ] <filename>     Output data filename\n"
+      << "  -s [ --softening ] <value>     Softening parameter (default 1e-4)\n"
+      << "  -e [ --eta ] <value>           ETA of time-step calculation (default 0.01)\n"
+      << "  -p [ --screen ]                Print summary in the screen instead of a file\n"
+      << "  -z [ --interval ] <value>      Output time interval (default 0.125)\n"
+      << "Extra options:\n"
+      << "  -l [ --lagrange ]              (accepted; Lagrange radii are not computed)\n"
+      << "  -a [ --all ]                   Print all the information of N-particles\n"
+      << "  -g [ --gpu ] <value> (=0)      GPUs to use (one GPU is used)\n"
+      << "  --mode fp64|exact|mixed        Force arithmetic (default fp64)\n"
+      << "  --host-steps                   Drive every block step from the host\n";
+    return s.str();
+}
+
+static bool is_opt(const char *a, const char *s, const char *l) {
+    return (s && std::strcmp(a, s) == 0) || std::strcmp(a, l) == 0;
+}
+
+bool OptionsParser::check_options() {
+    bool have_input = false, have_output = false;
+    std::string out;
+    for (int k = 1; k < argc_; k++) {
+        const char *a = argv_[k];
+        if (is_opt(a, "-h", "--help")) { std::cerr << usage() << std::endl; return false; }
+        if (is_opt(a, "-p", "--screen")) { ops.print_screen = true; continue; }
+        if (is_opt(a, "-a", "--all")) { ops.print_all = true; continue; }
+        if (is_opt(a, "-l", "--lagrange")) { ops.print_lagrange = true; continue; }
+        if (is_opt(a, nullptr, "--host-steps")) { host_steps = true; continue; }
+        static const char *with_value[][2] = {{"-i", "--input"}, {"-t", "--time"}, {"-o", "--output"},
+                                              {"-s", "--softening"}, {"-e", "--eta"}, {"-z", "--interval"},
+                                              {"-g", "--gpu"}, {nullptr, "--mode"}, {"-r", "--resume"}};
+        bool known = false;
+        for (auto &w : with_value) known = known || is_opt(a, w[0], w[1]);
+        if (!known) {
+            std::cerr << "gravidy: unknown option " << a << "\n" << usage() << std::endl;
+            return false;
+        }
+        if (k + 1 >= argc_) {
+            std::cerr << "gravidy: option requires an argument -- '" << a << "'" << std::endl;
+            return false;
+        }
+        const char *v = argv_[++k];
+        if (is_opt(a, "-i", "--input")) { input_filename = v; have_input = true; }
+        else if (is_opt(a, "-t", "--time")) integration_time = (float)std::strtod(v, nullptr);
+        else if (is_opt(a, "-o", "--output")) { out = v; have_output = true; }
+        else if (is_opt(a, "-s", "--softening")) softening = (float)std::strtod(v, nullptr);
+        else if (is_opt(a, "-e", "--eta")) eta = (float)std::strtod(v, nullptr);
+        else if (is_opt(a, "-z", "--interval")) interval_time = (float)std::strtod(v, nullptr);
+        else if (is_opt(a, "-g", "--gpu")) gpus = std::atoi(v);
+        else if (is_opt(a, nullptr, "--mode")) {
+            std::string m = v;
+            if (m == "fp64") force_mode = H4_FORCE_FP64;
+            else if (m == "exact") force_mode = H4_FORCE_EXACT;
+            else if (m == "mixed") force_mode = H4_FORCE_MIXED;
+            else { std::cerr << "gravidy: unknown --mode " << m << std::endl; return false; }
+        } else if (is_opt(a, "-r", "--resume")) {
+            std::cerr << "gravidy: --resume is not supported by this build" << std::endl;
+            return false;
+        } else {
+            std::cerr << "gravidy: unknown option " << a << "\n" << usage() << std::endl;
+            return false;
+        }
+    }
+    if (!have_input) {
+        std::cerr << "gravidy: option requires an argument -- 'input'" << std::endl << usage() << std::endl;
+        return false;
+    }
+    if (!file_exists(input_filename)) {
+        std::cerr << "gravidy: cannot access " << input_filename << ": No such file or directory" << std::endl;
+        return false;
+    }
+    if (!(integration_time > 0.0f) || !(interval_time > 0.0f) || !(eta > 0.0f) || !(softening >= 0.0f)) {
+        std::cerr << "gravidy: time, interval and eta must be > 0, softening >= 0" << std::endl;
+        return false;
+    }
+    // Digits of the snapshot counter (OptionsParser.cpp:392-399).
+    length_output_number = 0;
+    unsigned int tmp = (unsigned int)(integration_time / interval_time);
+    do {
+        ++length_output_number;
+        tmp /= 10;
+    } while (tmp);
+    length_output_number += 1;
+    output_filename = (have_output ? out : input_filename) + ".out";
+    return true;
+}
+
+}  // namespace gb300

@@ -1,0 +1,60 @@
+"""The gravidy-gb300 program (C++ drop-in of the reference's main flow) on
+the C1 input: its energy log against the reference program's own log."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from golden_util import case_dir, cases, load_cli_log
+from gravidy_gb300.build import CLI, build_cli, build_library
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(tmp_path, name, mode, extra=()):
+    build_library()
+    build_cli()
+    c = cases()[name]
+    out = os.path.join(str(tmp_path), "run")
+    cmd = [CLI, "-i", os.path.join(case_dir(name), "input.txt"), "-s", repr(c["softening"]),
+           "-e", repr(c["eta"]), "-t", repr(c["t_end"]), "-z", repr(c["interval"]), "-o", out,
+           "--mode", mode, *extra]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    rows = []
+    for line in open(out + ".out.log"):
+        if line.startswith("#"):
+            continue
+        t = line.split()
+        rows.append((t[1], t[2], t[3], float(t[4]), float(t[5]), float(t[6])))
+    return rows, out
+
+
+@pytest.mark.parametrize("extra", [(), ("--host-steps",)])
+def test_cli_exact_mode_energy_log_matches_reference(tmp_path, extra):
+    name = "c1_plummer_n1024"
+    rows, out = _run(tmp_path, name, "exact", extra)
+    ref = load_cli_log(name)
+    assert len(rows) == len(ref)
+    for mine, theirs in zip(rows, ref):
+        assert mine[:3] == theirs[:3]
+        assert abs(mine[3] - float(theirs[3])) <= 1e-10 * abs(float(theirs[3]))
+        assert abs(mine[5] - float(theirs[5])) <= 1e-5 * max(float(theirs[5]), 1e-12)
+    # snapshots and info file in the reference's layout
+    assert os.path.exists(out + ".out.info")
+    snaps = sorted(f for f in os.listdir(tmp_path) if ".snapshot_" in f)
+    assert len(snaps) == len(ref) + 1
+    with open(os.path.join(tmp_path, snaps[0])) as fh:
+        head = fh.readline()
+        assert head.startswith("# Time:")
+        assert len(fh.readline().split()) == 8
+
+
+def test_cli_fp64_energy_error_matches_reference(tmp_path):
+    name = "c1_plummer_n1024"
+    rows, _ = _run(tmp_path, name, "fp64")
+    ref = load_cli_log(name)
+    assert [r[0] for r in rows] == [r[0] for r in ref]
+    cum, cum_ref = rows[-1][5], float(ref[-1][5])
+    assert abs(cum - cum_ref) <= 1e-2 * cum_ref
