@@ -51,6 +51,19 @@ SIGNATURES = {
     "h4_kernel_launches": (_i, [_vp, C.POINTER(C.c_ulonglong)]),
     "h4_probe_peaks": (_i, [_pd, _pd]),
     "h4_forces_noalloc": (_i, [_u, _d, _vp, _vp, _u, _vp, _vp, _vp]),
+    "h4_ens_last_error": (C.c_char_p, []),
+    "h4_ens_create": (_i, [C.POINTER(_vp), _u, _vp, _vp, _vp, _vp, _vp, _i]),
+    "h4_ens_destroy": (_i, [_vp]),
+    "h4_ens_set_stream": (_i, [_vp, _vp]),
+    "h4_ens_set_tuning": (_i, [_vp, _vp, _vp]),
+    "h4_ens_set_dt_limits": (_i, [_vp, _d, _d]),
+    "h4_ens_init": (_i, [_vp]),
+    "h4_ens_advance": (_i, [_vp, _vp, _pd]),
+    "h4_ens_energy": (_i, [_vp, _vp, _vp]),
+    "h4_ens_download": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "h4_ens_system_stats": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "h4_ens_tune_force": (_i, [_vp, _u, _u, _u, C.POINTER(_f)]),
+    "h4_ens_timings": (_i, [_vp, C.POINTER(_f), C.POINTER(C.c_ulonglong)]),
     "h4_forces_noalloc_error": (C.c_char_p, []),
 }
 
@@ -86,6 +99,12 @@ def check(status: int) -> None:
     if status != H4_OK:
         L = load()
         raise H4Error(status, L.h4_last_error().decode() or L.h4_status_string(status).decode())
+
+
+def check_ens(status: int) -> None:
+    if status != H4_OK:
+        L = load()
+        raise H4Error(status, L.h4_ens_last_error().decode() or L.h4_status_string(status).decode())
 
 
 def ptr(a: np.ndarray | None):

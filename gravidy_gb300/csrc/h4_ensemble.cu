@@ -1,0 +1,932 @@
+// Batched ensemble: many independent N-body systems (star clusters of uneven
+// N), each with its own block time and active set, advanced together by one
+// persistent fused kernel per graph iteration.
+//
+// The per-system arithmetic is the single-system path's (exact-order
+// predictor/corrector/timestep of h4_exact.cuh, force items of h4_pair.cuh);
+// what changes is the schedule.  One iteration of k_ensemble does one block
+// step of every unfinished system, in three phases separated by grid-wide
+// barriers:
+//   P0  per system (one block): block time = next time, ordered active set,
+//       predictor of all its particles, force work layout from the tuning
+//       table (particles per warp item, j-chunk length) for its (N, N_act);
+//   P1  all blocks: warp items of every system's force sum, taken from one
+//       global work queue (the systems' item counts are prefix-summed in
+//       shared memory; an item finds its system by binary search);
+//   P2  per system (the same block as P0): fixed-order reduction of the
+//       partial forces, save of the old forces, corrector, new timesteps, and
+//       the system's next block time.
+// The kernel is launched cooperatively (all blocks resident), and its grid
+// barriers are bounded waits on the global timer: a barrier that waits longer
+// than BARRIER_TIMEOUT_NS records H4_ERRBIT_TIMEOUT and every block leaves.
+// A CUDA graph with a device-side while loop relaunches the kernel until
+// every system has reached its end time.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gravidy_gb300.h"
+#include "h4_exact.cuh"
+#include "h4_internal.cuh"
+#include "h4_pair.cuh"
+
+namespace h4 {
+namespace ens {
+
+constexpr int THREADS = 256;
+constexpr int WARPS = THREADS / 32;
+constexpr int NB_N = H4_ENS_TUNE_NB_N;
+constexpr int NB_A = H4_ENS_TUNE_NB_A;
+constexpr unsigned long long BARRIER_TIMEOUT_NS = 60ull * 1000000000ull;
+constexpr int ITERS_PER_LAUNCH = 16;
+constexpr unsigned MAX_SYSTEMS = 8192;
+
+struct System {
+    int off, n;                  // particle offset and count
+    double e2, eta, dt_min, dt_max;
+    double t_end;
+    double itime, atime;         // last block time, next block time
+    unsigned nact;
+    unsigned ig, chunk, split, n_groups, items;
+    unsigned done, err;
+    size_t part_off, part_cap;   // partial-force area (doubles)
+    unsigned long long steps, psteps, inter;
+};
+
+struct Dev {
+    int nsys, total;
+    System *sys;
+    dbl4 *r, *v, *pr, *pv;
+    double *f, *old, *a2, *a3, *t, *dt;
+    float4 *jf0, *jf1, *jf2;
+    unsigned *move;
+    double *part;
+    unsigned *queue;             // force work-queue head
+    unsigned *bar_count, *bar_gen;
+    unsigned *err;               // global error bits
+    unsigned *tune_ig, *tune_chunk;   // [NB_N * NB_A]
+    unsigned *forced_nact;       // tuning probe: active count forced on every system (0 = off)
+    unsigned long long *launches;     // persistent-kernel launches so far
+    unsigned long long max_launches;
+    double *epot_i, *energy;     // energy: per particle, per system (kin, pot)
+    int mode;
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid-wide barrier of a cooperative launch, bounded in time.
+__device__ bool grid_sync(const Dev &d) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = d.bar_gen;
+        const unsigned g0 = *gen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(d.bar_count, 1u) + 1u;
+        if (arrived == gridDim.x) {
+            *d.bar_count = 0u;
+            __threadfence();
+            atomicAdd((unsigned *)d.bar_gen, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            while (*gen == g0) {
+                if (global_ns() - t0 > BARRIER_TIMEOUT_NS) {
+                    atomicOr(d.err, (unsigned)H4_ERRBIT_TIMEOUT);
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return (*(volatile unsigned *)d.err & H4_ERRBIT_TIMEOUT) == 0u;
+}
+
+__device__ __forceinline__ int n_bucket(int n) {
+    int b = 0;
+    for (int lim = 512; b < NB_N - 1 && n > lim; lim <<= 1) b++;
+    return b;
+}
+__device__ __forceinline__ int a_bucket(unsigned nact) {
+    // 1 | 2-3 | 4-15 | 16-63 | 64-255 | 256-1023 | 1024-4095 | >= 4096
+    if (nact <= 1) return 0;
+    int b = 1;
+    for (unsigned lim = 4; b < NB_A - 1 && nact >= lim; lim <<= 2) b++;
+    return b;
+}
+
+__device__ unsigned block_sum_u(unsigned x, unsigned *red) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    __syncthreads();
+    if (lane == 0) red[w] = x;
+    __syncthreads();
+    unsigned s = 0;
+    for (int k = 0; k < WARPS; k++) s += red[k];
+    __syncthreads();
+    return s;
+}
+
+// Exclusive scan of one value per thread (THREADS threads).
+__device__ unsigned block_scan_u(unsigned x, unsigned *red, unsigned *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    __syncthreads();
+    if (lane == 31) red[w] = incl;
+    __syncthreads();
+    unsigned before = 0, all = 0;
+    for (int k = 0; k < WARPS; k++) {
+        if (k < w) before += red[k];
+        all += red[k];
+    }
+    *total = all;
+    __syncthreads();
+    return before + incl - x;
+}
+
+// ---- P0: active set, predictor, work layout of one system -------------------
+template <int MODE>
+__device__ void phase0(const Dev &d, int c, bool init, unsigned *red) {
+    System &S = d.sys[c];
+    if (S.done) {
+        if (threadIdx.x == 0) S.items = 0;
+        return;
+    }
+    const int off = S.off, n = S.n;
+    const double itime = init ? 0.0 : S.atime;
+    unsigned nact = 0;
+    const unsigned forced = *d.forced_nact;
+    if (init || forced) {
+        const int na = init ? n : (int)min((unsigned)n, forced);
+        for (int i = threadIdx.x; i < na; i += THREADS) d.move[off + i] = (unsigned)i;
+        nact = (unsigned)na;
+    } else {
+        // ascending compaction, 8 particles per thread per round
+        for (int base = 0; base < n; base += THREADS * 8) {
+            unsigned flags = 0, cnt = 0;
+            const int i0 = base + threadIdx.x * 8;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int i = i0 + q;
+                if (i < n && exact::is_active(itime, d.t[off + i], d.dt[off + i])) {
+                    flags |= 1u << q;
+                    cnt++;
+                }
+            }
+            unsigned tot;
+            unsigned pos = nact + block_scan_u(cnt, red, &tot);
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+                if (flags & (1u << q)) d.move[off + pos++] = (unsigned)(i0 + q);
+            nact += tot;
+        }
+    }
+    // predictor of all particles (init: the state itself, Hermite4::init_data)
+    for (int i = threadIdx.x; i < n; i += THREADS) {
+        const int g = off + i;
+        dbl4 pr, pv;
+        if (init || forced) {
+            pr = d.r[g];
+            pr.w = (double)(float)pr.w;
+            pv = d.v[g];
+            pv.w = 0.0;
+        } else {
+            exact::predict(itime, d.t[g], d.f + 6 * (size_t)g, d.r[g], d.v[g], pr, pv);
+        }
+        d.pr[g] = pr;
+        d.pv[g] = pv;
+        if (MODE == H4_FORCE_MIXED) {
+            float4 a, b, cc;
+            exact::pack_jf(pr, pv, a, b, cc);
+            d.jf0[g] = a;
+            d.jf1[g] = b;
+            d.jf2[g] = cc;
+        }
+    }
+    if (threadIdx.x == 0) {
+        if (!forced) S.itime = itime;   // a tuning probe leaves the block time alone
+        S.nact = nact;
+        unsigned ig, chunk, split;
+        if (MODE == H4_FORCE_EXACT) {
+            ig = 32; chunk = (unsigned)n; split = 1;
+        } else {
+            const int t = n_bucket(n) * NB_A + a_bucket(nact);
+            ig = d.tune_ig[t];
+            chunk = d.tune_chunk[t];
+            if (ig != 1 && ig != 2 && ig != 4) ig = 4;
+            chunk = max(32u, (chunk + 31u) & ~31u);
+            split = ((unsigned)n + chunk - 1) / chunk;
+            const unsigned cap = nact ? (unsigned)(S.part_cap / (6ull * nact)) : 1u;
+            if (split > cap) {
+                split = max(1u, cap);
+                chunk = (((unsigned)n + split - 1) / split + 31u) & ~31u;
+                split = ((unsigned)n + chunk - 1) / chunk;
+            }
+        }
+        S.ig = ig;
+        S.chunk = chunk;
+        S.split = split;
+        S.n_groups = nact ? (nact + ig - 1) / ig : 0;
+        S.items = S.n_groups * split;
+    }
+}
+
+// ---- P1: one warp item of some system's force sum ---------------------------
+template <int MODE>
+__device__ void force_item(const Dev &d, const System &S, unsigned local, int lane) {
+    const unsigned s = local / S.n_groups;
+    const unsigned g = local - s * S.n_groups;
+    const int off = S.off;
+    const int jb = (int)(s * S.chunk);
+    const int je = min(S.n, jb + (int)S.chunk);
+    const unsigned nact = S.nact;
+    double *part_s = d.part + S.part_off + (size_t)s * 6 * nact;
+    const unsigned *move = d.move + off;
+    if (MODE == H4_FORCE_EXACT) {
+        const unsigned k = g * 32 + lane;
+        if (k < nact) {
+            double f[6];
+            pair::exact_sum(d.pr + off, d.pv + off, S.n, move[k], S.e2, f);
+#pragma unroll
+            for (int c = 0; c < 6; c++) part_s[(size_t)c * nact + k] = f[c];
+        }
+        return;
+    }
+    const unsigned k0 = g * S.ig;
+    const unsigned cnt = min(S.ig, nact - k0);
+    if (MODE == H4_FORCE_FP64) {
+        const dbl4 *pr = d.pr + off, *pv = d.pv + off;
+        if (cnt == 4) {
+            pair::fp64_warp_item<4>(pr, pv, move, nact, k0, jb, je, S.e2, part_s, lane);
+        } else {
+            unsigned k = k0;
+            if (cnt >= 2) { pair::fp64_warp_item<2>(pr, pv, move, nact, k, jb, je, S.e2, part_s, lane); k += 2; }
+            if (cnt & 1) pair::fp64_warp_item<1>(pr, pv, move, nact, k, jb, je, S.e2, part_s, lane);
+        }
+    } else {
+        const float4 *a = d.jf0 + off, *b = d.jf1 + off, *c = d.jf2 + off;
+        const float e2 = (float)S.e2;
+        if (S.e2 > 0.0) {
+            if (cnt == 4) {
+                pair::mixed_warp_item<4, false>(a, b, c, move, nact, k0, jb, je, e2, part_s, lane);
+            } else {
+                unsigned k = k0;
+                if (cnt >= 2) { pair::mixed_warp_item<2, false>(a, b, c, move, nact, k, jb, je, e2, part_s, lane); k += 2; }
+                if (cnt & 1) pair::mixed_warp_item<1, false>(a, b, c, move, nact, k, jb, je, e2, part_s, lane);
+            }
+        } else {
+            unsigned k = k0;
+            while (k < k0 + cnt) {
+                pair::mixed_warp_item<1, true>(a, b, c, move, nact, k, jb, je, e2, part_s, lane);
+                k++;
+            }
+        }
+    }
+}
+
+// ---- P2: reduction, corrector, timesteps, next time of one system -----------
+__device__ void phase2(const Dev &d, int c, bool init, double *redd) {
+    System &S = d.sys[c];
+    if (S.done) return;
+    const int off = S.off, n = S.n;
+    const unsigned nact = S.nact, split = S.split;
+    const double itime = S.itime;
+    bool bad = false;
+    for (unsigned k = threadIdx.x; k < nact; k += THREADS) {
+        const unsigned i = d.move[off + k];
+        const size_t g = (size_t)off + i;
+        double fn[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) fn[q] = 0.0;
+        for (unsigned s = 0; s < split; s++) {
+            const double *p = d.part + S.part_off + (size_t)s * 6 * nact;
+#pragma unroll
+            for (int q = 0; q < 6; q++) fn[q] = exact::add(fn[q], p[(size_t)q * nact + k]);
+        }
+        double *fp = d.f + 6 * g;
+        if (init) {
+#pragma unroll
+            for (int q = 0; q < 6; q++) fp[q] = fn[q];
+            d.dt[g] = exact::init_dt(fn, (double)0.01f, S.dt_min, S.dt_max);
+            d.t[g] = 0.0;
+            continue;
+        }
+        double o[6];
+        double *op = d.old + 6 * g;
+#pragma unroll
+        for (int q = 0; q < 6; q++) { o[q] = fp[q]; op[q] = o[q]; fp[q] = fn[q]; }
+        dbl4 r = d.r[g], v = d.v[g];
+        double a2[3], a3[3], ndt;
+        const bool ok = exact::correct(itime, S.eta, S.dt_min, S.dt_max, fn, o, d.pr[g], d.pv[g], d.dt[g], r, v,
+                                       a2, a3, ndt);
+        d.r[g] = r;
+        d.v[g] = v;
+#pragma unroll
+        for (int q = 0; q < 3; q++) { d.a2[3 * g + q] = a2[q]; d.a3[3 * g + q] = a3[q]; }
+        d.t[g] = itime;
+        d.dt[g] = ndt;
+        bad |= !ok;
+    }
+    __syncthreads();
+    // next block time of this system: min (t + dt)
+    double m = __longlong_as_double((long long)exact::INF_BITS);
+    for (int i = threadIdx.x; i < n; i += THREADS) m = fmin(m, exact::add(d.t[off + i], d.dt[off + i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, o));
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) redd[w] = m;
+    const int anybad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < WARPS; k++) m = fmin(m, redd[k]);
+        S.atime = m;
+        if (!init) {
+            S.steps += 1;
+            S.psteps += nact;
+            S.inter += (unsigned long long)nact * (unsigned long long)n;
+        }
+        if (anybad) {
+            S.err |= H4_ERRBIT_NONFINITE;
+            atomicOr(d.err, (unsigned)H4_ERRBIT_NONFINITE);
+        }
+        S.done = (anybad || !(itime < S.t_end)) ? 1u : 0u;
+        if (init) S.done = (0.0 < S.t_end) ? 0u : 1u;
+    }
+    __syncthreads();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(THREADS) k_ensemble(Dev d, int iters, int init, int force_only) {
+    extern __shared__ unsigned s_prefix[];   // [nsys + 1]
+    __shared__ unsigned red[WARPS];
+    __shared__ double redd[WARPS];
+    __shared__ unsigned s_item[WARPS];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int it = 0; it < iters; it++) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            *d.queue = 0u;
+            __threadfence();
+        }
+        for (int c = blockIdx.x; c < d.nsys; c += gridDim.x) phase0<MODE>(d, c, init != 0, red);
+        if (!grid_sync(d)) return;
+        // prefix of the systems' item counts
+        unsigned carry = 0;
+        for (int base = 0; base < d.nsys; base += THREADS) {
+            const int c = base + threadIdx.x;
+            const unsigned x = c < d.nsys ? d.sys[c].items : 0u;
+            unsigned tot;
+            const unsigned ex = block_scan_u(x, red, &tot);
+            if (c < d.nsys) s_prefix[c] = carry + ex;
+            carry += tot;
+        }
+        if (threadIdx.x == 0) s_prefix[d.nsys] = carry;
+        __syncthreads();
+        const unsigned total = carry;
+        for (;;) {
+            if (lane == 0) s_item[w] = atomicAdd(d.queue, 1u);
+            __syncwarp();
+            const unsigned item = s_item[w];
+            __syncwarp();
+            if (item >= total) break;
+            int lo = 0, hi = d.nsys;   // last c with s_prefix[c] <= item
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (s_prefix[mid] <= item) lo = mid; else hi = mid;
+            }
+            force_item<MODE>(d, d.sys[lo], item - s_prefix[lo], lane);
+        }
+        if (!grid_sync(d)) return;
+        if (force_only) return;
+        for (int c = blockIdx.x; c < d.nsys; c += gridDim.x) phase2(d, c, init != 0, redd);
+    }
+}
+
+// Loop condition of the graph: continue while a system is unfinished, no
+// error was recorded and the launch bound is not reached.
+__global__ void k_ens_check(Dev d, cudaGraphConditionalHandle cond) {
+    __shared__ unsigned any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < d.nsys; c += blockDim.x)
+        if (!d.sys[c].done) any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned long long l = ++*d.launches;
+        unsigned go = any && (*d.err == 0u);
+        if (go && l >= d.max_launches) {
+            atomicOr(d.err, (unsigned)H4_ERRBIT_STEPCAP);
+            go = 0;
+        }
+        cudaGraphSetConditional(cond, go);
+    }
+}
+
+// Energy of every system: ring pairing (as h4_energy.cu) over warp items of
+// 4 particles, then a fixed-order sum per system (one block per system).
+__global__ void __launch_bounds__(THREADS) k_ens_energy_pairs(Dev d) {
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
+    const int nw = gridDim.x * WARPS;
+    int item = gw;
+    for (int c = 0; c < d.nsys; c++) {
+        const System &S = d.sys[c];
+        const int n = S.n, off = S.off;
+        const int groups = (n + 3) / 4;
+        for (; item < groups; item += nw) {
+            const int i0 = item * 4;
+            const int half = n / 2;
+            const bool even = (n % 2) == 0;
+            double acc[4];
+            int ie[4];
+            double xi[4], yi[4], zi[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                ie[q] = min(i0 + q, n - 1);
+                const dbl4 r = d.r[off + ie[q]];
+                xi[q] = r.x; yi[q] = r.y; zi[q] = r.z;
+                acc[q] = 0.0;
+            }
+            for (int o = 1 + lane; o <= half; o += 32) {
+                const double wgt = (even && o == half) ? 0.5 : 1.0;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    int j = ie[q] + o;
+                    if (j >= n) j -= n;
+                    const dbl4 rj = d.r[off + j];
+                    const double dx = rj.x - xi[q], dy = rj.y - yi[q], dz = rj.z - zi[q];
+                    acc[q] = fma(wgt * rj.w, pair::rsqrt_refined(fma(dx, dx, fma(dy, dy, dz * dz))), acc[q]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                double a = acc[q];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+                if (lane == 0 && i0 + q < n) d.epot_i[off + i0 + q] = n > 1 ? -a * d.r[off + i0 + q].w : 0.0;
+            }
+        }
+        item -= groups;
+    }
+}
+
+__global__ void __launch_bounds__(THREADS) k_ens_energy_sum(Dev d) {
+    __shared__ double sk[THREADS], sp[THREADS];
+    for (int c = blockIdx.x; c < d.nsys; c += gridDim.x) {
+        const System &S = d.sys[c];
+        double ek = 0.0, ep = 0.0;
+        for (int i = threadIdx.x; i < S.n; i += THREADS) {
+            const dbl4 v = d.v[S.off + i];
+            ek += 0.5 * d.r[S.off + i].w * (v.x * v.x + v.y * v.y + v.z * v.z);
+            ep += d.epot_i[S.off + i];
+        }
+        sk[threadIdx.x] = ek;
+        sp[threadIdx.x] = ep;
+        __syncthreads();
+        for (int s = THREADS / 2; s > 0; s >>= 1) {
+            if ((int)threadIdx.x < s) {
+                sk[threadIdx.x] += sk[threadIdx.x + s];
+                sp[threadIdx.x] += sp[threadIdx.x + s];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            d.energy[2 * c] = sk[0];
+            d.energy[2 * c + 1] = sp[0];
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace ens
+}  // namespace h4
+
+// ============================== host side =====================================
+using namespace h4;
+using namespace h4::ens;
+
+namespace {
+thread_local std::string g_ens_err;
+int efail(int st, const std::string &m) {
+    g_ens_err = m;
+    return st;
+}
+int ecuda(cudaError_t e, const char *what) {
+    g_ens_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return H4_ERR_CUDA;
+}
+#define ENS_TRY(call, what)                        \
+    do {                                           \
+        cudaError_t e__ = (call);                  \
+        if (e__ != cudaSuccess) return ecuda(e__, what); \
+    } while (0)
+}  // namespace
+
+struct h4_ensemble_s {
+    Dev d{};
+    int nsys = 0, total = 0, mode = 0, num_sms = 0, grid = 0;
+    size_t smem = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    std::vector<System> host_sys;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float last_ms = 0.f;
+    unsigned long long launches = 0;
+    bool initialised = false;
+    std::vector<void *> allocs;
+};
+
+namespace {
+
+template <int MODE>
+const void *ens_kernel() { return (const void *)k_ensemble<MODE>; }
+
+const void *kernel_for(int mode) {
+    switch (mode) {
+    case H4_FORCE_EXACT: return ens_kernel<H4_FORCE_EXACT>();
+    case H4_FORCE_MIXED: return ens_kernel<H4_FORCE_MIXED>();
+    default: return ens_kernel<H4_FORCE_FP64>();
+    }
+}
+
+cudaError_t launch_persistent(h4_ensemble_s *E, cudaStream_t s, int iters, int init, int force_only) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)E->grid);
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = E->smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void *args[] = {(void *)&E->d, (void *)&iters, (void *)&init, (void *)&force_only};
+    return cudaLaunchKernelExC(&cfg, kernel_for(E->mode), args);
+}
+
+template <typename T>
+cudaError_t dalloc(h4_ensemble_s *E, T **p, size_t count) {
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (count ? count : 1));
+    if (e == cudaSuccess) E->allocs.push_back((void *)*p);
+    return e;
+}
+
+void ens_free(h4_ensemble_s *E) {
+    if (E->exec) cudaGraphExecDestroy(E->exec);
+    if (E->graph) cudaGraphDestroy(E->graph);
+    if (E->cap) cudaStreamDestroy(E->cap);
+    if (E->e0) cudaEventDestroy(E->e0);
+    if (E->e1) cudaEventDestroy(E->e1);
+    for (void *p : E->allocs) cudaFree(p);
+    if (E->own) cudaStreamDestroy(E->own);
+}
+
+// Default tuning table: up to 4 particles per warp item; j-chunks short for
+// small active sets (more items), the whole system for large ones.
+void default_tuning(unsigned *ig, unsigned *chunk) {
+    for (int b = 0; b < NB_N; b++) {
+        for (int a = 0; a < NB_A; a++) {
+            const int t = b * NB_A + a;
+            ig[t] = 4;
+            static const unsigned ch[NB_A] = {128, 128, 256, 512, 1024, 2048, 4096, 8192};
+            chunk[t] = ch[a];
+        }
+    }
+}
+
+int build_ens_graph(h4_ensemble_s *E) {
+    if (E->exec) return H4_OK;
+    if (!E->cap) ENS_TRY(cudaStreamCreateWithFlags(&E->cap, cudaStreamNonBlocking), "ensemble capture stream");
+    ENS_TRY(cudaGraphCreate(&E->graph, 0), "cudaGraphCreate");
+    cudaGraphConditionalHandle cond;
+    ENS_TRY(cudaGraphConditionalHandleCreate(&cond, E->graph, 1u, cudaGraphCondAssignDefault), "conditional handle");
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    ENS_TRY(cudaGraphAddNode(&node, E->graph, nullptr, nullptr, 0, &cp), "while node");
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    ENS_TRY(cudaStreamBeginCaptureToGraph(E->cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+            "begin capture");
+    cudaError_t e = launch_persistent(E, E->cap, ITERS_PER_LAUNCH, 0, 0);
+    if (e == cudaSuccess) {
+        k_ens_check<<<1, 256, 0, E->cap>>>(E->d, cond);
+        e = cudaGetLastError();
+    }
+    cudaGraph_t out = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(E->cap, &out);
+    if (e != cudaSuccess) return ecuda(e, "capture ensemble step");
+    if (e2 != cudaSuccess) return ecuda(e2, "end capture");
+    ENS_TRY(cudaGraphInstantiate(&E->exec, E->graph, 0), "instantiate ensemble graph");
+    return H4_OK;
+}
+
+int pull_systems(h4_ensemble_s *E) {
+    ENS_TRY(cudaMemcpyAsync(E->host_sys.data(), E->d.sys, sizeof(System) * E->nsys, cudaMemcpyDeviceToHost,
+                            E->stream),
+            "copy systems");
+    ENS_TRY(cudaStreamSynchronize(E->stream), "synchronize");
+    return H4_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *h4_ens_last_error(void) { return g_ens_err.c_str(); }
+
+int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, const double *e2, const float *eta,
+                  const h4_double4 *r, const h4_double4 *v, int mode) {
+    if (!out) return efail(H4_ERR_ARG, "h4_ens_create: out is NULL");
+    *out = nullptr;
+    if (nsys < 1 || nsys > MAX_SYSTEMS) return efail(H4_ERR_ARG, "h4_ens_create: nsys must be in [1, 8192]");
+    if (!n || !e2 || !eta || !r || !v) return efail(H4_ERR_ARG, "h4_ens_create: null array");
+    if (mode < H4_FORCE_FP64 || mode > H4_FORCE_MIXED) return efail(H4_ERR_ARG, "h4_ens_create: unknown mode");
+    size_t total = 0, part_total = 0;
+    for (unsigned c = 0; c < nsys; c++) {
+        if (n[c] < 1 || n[c] > (1u << 24)) return efail(H4_ERR_ARG, "h4_ens_create: system size out of range");
+        if (!(e2[c] >= 0.0) || !(eta[c] > 0.f)) return efail(H4_ERR_ARG, "h4_ens_create: bad e2 or eta");
+        total += n[c];
+        part_total += 6 * ((size_t)n[c] + 4096);
+    }
+    if (total > (1u << 28)) return efail(H4_ERR_ARG, "h4_ens_create: too many particles");
+    for (size_t i = 0; i < total; i++)
+        if (!std::isfinite(r[i].x) || !std::isfinite(r[i].y) || !std::isfinite(r[i].z) || !std::isfinite(r[i].w) ||
+            !std::isfinite(v[i].x) || !std::isfinite(v[i].y) || !std::isfinite(v[i].z))
+            return efail(H4_ERR_NONFINITE, "h4_ens_create: non-finite input at particle " + std::to_string(i));
+    h4_ensemble_s *E = new (std::nothrow) h4_ensemble_s();
+    if (!E) return efail(H4_ERR_ALLOC, "h4_ens_create: host allocation");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&E->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) { delete E; return ecuda(e, "h4_ens_create: no CUDA device"); }
+    E->nsys = (int)nsys;
+    E->total = (int)total;
+    E->mode = mode;
+    Dev &d = E->d;
+    d.nsys = (int)nsys;
+    d.total = (int)total;
+    d.mode = mode;
+    E->host_sys.resize(nsys);
+    size_t off = 0, poff = 0;
+    for (unsigned c = 0; c < nsys; c++) {
+        System S{};
+        S.off = (int)off;
+        S.n = (int)n[c];
+        S.e2 = e2[c];
+        S.eta = (double)eta[c];
+        S.dt_min = 1.1920928955078125e-07;
+        S.dt_max = 0.125;
+        S.t_end = 0.0;
+        S.part_off = poff;
+        S.part_cap = 6 * ((size_t)n[c] + 4096);
+        E->host_sys[c] = S;
+        off += n[c];
+        poff += S.part_cap;
+    }
+    e = cudaSuccess;
+#define EA(p, cnt) if (e == cudaSuccess) e = dalloc(E, &p, cnt)
+    EA(d.sys, nsys); EA(d.r, total); EA(d.v, total); EA(d.pr, total); EA(d.pv, total);
+    EA(d.f, 6 * total); EA(d.old, 6 * total); EA(d.a2, 3 * total); EA(d.a3, 3 * total);
+    EA(d.t, total); EA(d.dt, total); EA(d.move, total); EA(d.part, part_total);
+    EA(d.queue, 1); EA(d.bar_count, 1); EA(d.bar_gen, 1); EA(d.err, 1);
+    EA(d.tune_ig, NB_N * NB_A); EA(d.tune_chunk, NB_N * NB_A); EA(d.forced_nact, 1); EA(d.launches, 1);
+    EA(d.epot_i, total); EA(d.energy, 2 * nsys);
+    if (mode == H4_FORCE_MIXED) { EA(d.jf0, total); EA(d.jf1, total); EA(d.jf2, total); }
+#undef EA
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->own, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&E->e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&E->e1);
+    if (e != cudaSuccess) { ens_free(E); delete E; return efail(H4_ERR_ALLOC, std::string("h4_ens_create: ") + cudaGetErrorString(e)); }
+    E->stream = E->own;
+    cudaStream_t s = E->stream;
+    std::vector<h4_double4> rr(r, r + total);
+    for (auto &p : rr) p.w = (double)(float)p.w;   // masses are floats in the reference
+    std::vector<unsigned> tig(NB_N * NB_A), tch(NB_N * NB_A);
+    default_tuning(tig.data(), tch.data());
+    e = cudaMemcpy(d.sys, E->host_sys.data(), sizeof(System) * nsys, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d.r, rr.data(), sizeof(dbl4) * total, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d.v, v, sizeof(dbl4) * total, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d.tune_ig, tig.data(), sizeof(unsigned) * tig.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d.tune_chunk, tch.data(), sizeof(unsigned) * tch.size(), cudaMemcpyHostToDevice);
+    void *zero[] = {d.f, d.old, d.a2, d.a3, d.t, d.dt};
+    size_t zb[] = {48 * total, 48 * total, 24 * total, 24 * total, 8 * total, 8 * total};
+    for (int k = 0; k < 6 && e == cudaSuccess; k++) e = cudaMemsetAsync(zero[k], 0, zb[k], s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.queue, 0, 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.bar_count, 0, 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.bar_gen, 0, 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.err, 0, 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.forced_nact, 0, 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.launches, 0, 8, s);
+    // persistent grid: every block resident (cooperative launch)
+    E->smem = sizeof(unsigned) * (nsys + 1);
+    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel_for(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel_for(mode), THREADS, E->smem);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess || per_sm < 1) {
+        ens_free(E);
+        delete E;
+        return e != cudaSuccess ? ecuda(e, "h4_ens_create: setup") : efail(H4_ERR_CUDA, "h4_ens_create: kernel does not fit an SM");
+    }
+    E->grid = E->num_sms * std::min(per_sm, 2);
+    *out = E;
+    return H4_OK;
+}
+
+int h4_ens_destroy(h4_ens_handle E) {
+    if (!E) return H4_OK;
+    cudaStreamSynchronize(E->stream);
+    ens_free(E);
+    delete E;
+    return H4_OK;
+}
+
+int h4_ens_set_stream(h4_ens_handle E, void *stream) {
+    if (!E) return efail(H4_ERR_ARG, "null handle");
+    ENS_TRY(cudaStreamSynchronize(E->stream), "synchronize");
+    E->stream = stream ? (cudaStream_t)stream : E->own;
+    return H4_OK;
+}
+
+int h4_ens_set_tuning(h4_ens_handle E, const unsigned int *ig, const unsigned int *chunk) {
+    if (!E || !ig || !chunk) return efail(H4_ERR_ARG, "h4_ens_set_tuning: null argument");
+    for (int t = 0; t < NB_N * NB_A; t++)
+        if ((ig[t] != 1 && ig[t] != 2 && ig[t] != 4) || chunk[t] < 32 || chunk[t] > (1u << 24))
+            return efail(H4_ERR_ARG, "h4_ens_set_tuning: ig must be 1, 2 or 4 and chunk in [32, 2^24]");
+    ENS_TRY(cudaMemcpyAsync(E->d.tune_ig, ig, sizeof(unsigned) * NB_N * NB_A, cudaMemcpyHostToDevice, E->stream), "tuning");
+    ENS_TRY(cudaMemcpyAsync(E->d.tune_chunk, chunk, sizeof(unsigned) * NB_N * NB_A, cudaMemcpyHostToDevice, E->stream), "tuning");
+    ENS_TRY(cudaStreamSynchronize(E->stream), "tuning");
+    return H4_OK;
+}
+
+int h4_ens_set_dt_limits(h4_ens_handle E, double dt_min, double dt_max) {
+    if (!E) return efail(H4_ERR_ARG, "null handle");
+    int ex1, ex2;
+    if (!(dt_min > 0) || !(dt_max >= dt_min) || std::frexp(dt_min, &ex1) != 0.5 || std::frexp(dt_max, &ex2) != 0.5)
+        return efail(H4_ERR_ARG, "h4_ens_set_dt_limits: powers of two with dt_min <= dt_max");
+    int st = pull_systems(E);
+    if (st) return st;
+    for (auto &S : E->host_sys) { S.dt_min = dt_min; S.dt_max = dt_max; }
+    ENS_TRY(cudaMemcpyAsync(E->d.sys, E->host_sys.data(), sizeof(System) * E->nsys, cudaMemcpyHostToDevice, E->stream), "systems");
+    ENS_TRY(cudaStreamSynchronize(E->stream), "systems");
+    return H4_OK;
+}
+
+int h4_ens_init(h4_ens_handle E) {
+    if (!E) return efail(H4_ERR_ARG, "null handle");
+    int st = pull_systems(E);
+    if (st) return st;
+    for (auto &S : E->host_sys) { S.done = 0; S.t_end = 1.0; S.steps = S.psteps = S.inter = 0; S.err = 0; }
+    ENS_TRY(cudaMemcpyAsync(E->d.sys, E->host_sys.data(), sizeof(System) * E->nsys, cudaMemcpyHostToDevice, E->stream), "systems");
+    ENS_TRY(launch_persistent(E, E->stream, 1, 1, 0), "h4_ens_init launch");
+    E->launches += 1;
+    ENS_TRY(cudaStreamSynchronize(E->stream), "h4_ens_init");
+    unsigned err = 0;
+    ENS_TRY(cudaMemcpy(&err, E->d.err, 4, cudaMemcpyDeviceToHost), "error word");
+    if (err) return efail(H4_ERR_CUDA, "h4_ens_init: device error bits " + std::to_string(err));
+    E->initialised = true;
+    return H4_OK;
+}
+
+int h4_ens_advance(h4_ens_handle E, const double *t_end, double stats[4]) {
+    if (!E || !t_end) return efail(H4_ERR_ARG, "h4_ens_advance: null argument");
+    if (!E->initialised) return efail(H4_ERR_STATE, "h4_ens_advance: call h4_ens_init first");
+    int st = pull_systems(E);
+    if (st) return st;
+    unsigned long long before_steps = 0;
+    double span = 0.0, dtmin = 1.0;
+    for (int c = 0; c < E->nsys; c++) {
+        System &S = E->host_sys[c];
+        before_steps += S.steps;
+        S.t_end = t_end[c];
+        S.done = (S.err || !(S.itime < S.t_end)) ? 1u : 0u;
+        if (S.steps == 0) S.done = (S.t_end > 0.0 && !S.err) ? 0u : 1u;
+        span = std::max(span, S.t_end - S.itime);
+        dtmin = std::min(dtmin, S.dt_min);
+    }
+    ENS_TRY(cudaMemcpyAsync(E->d.sys, E->host_sys.data(), sizeof(System) * E->nsys, cudaMemcpyHostToDevice, E->stream), "systems");
+    // Launch bound: every iteration advances each unfinished system by at
+    // least dt_min, so span/dt_min iterations always suffice.
+    const double iters = span / dtmin + 16.0;
+    E->d.max_launches = (unsigned long long)std::min(iters / ITERS_PER_LAUNCH + 2.0, 1.0e12);
+    ENS_TRY(cudaMemsetAsync(E->d.launches, 0, 8, E->stream), "launch counter");
+    if (E->exec) { cudaGraphExecDestroy(E->exec); E->exec = nullptr; cudaGraphDestroy(E->graph); E->graph = nullptr; }
+    st = build_ens_graph(E);
+    if (st) return st;
+    cudaEventRecord(E->e0, E->stream);
+    ENS_TRY(cudaGraphLaunch(E->exec, E->stream), "ensemble graph launch");
+    cudaEventRecord(E->e1, E->stream);
+    if ((st = pull_systems(E))) return st;
+    cudaEventElapsedTime(&E->last_ms, E->e0, E->e1);
+    unsigned long long nl = 0;
+    unsigned err = 0;
+    ENS_TRY(cudaMemcpy(&nl, E->d.launches, 8, cudaMemcpyDeviceToHost), "launch counter");
+    ENS_TRY(cudaMemcpy(&err, E->d.err, 4, cudaMemcpyDeviceToHost), "error word");
+    E->launches += 2 * nl;
+    unsigned long long steps = 0, ps = 0, inter = 0;
+    for (auto &S : E->host_sys) { steps += S.steps; ps += S.psteps; inter += S.inter; }
+    if (stats) {
+        stats[0] = (double)(steps - before_steps);
+        stats[1] = (double)ps;
+        stats[2] = (double)inter;
+        stats[3] = (double)nl;
+    }
+    if (err & H4_ERRBIT_TIMEOUT) return efail(H4_ERR_CUDA, "h4_ens_advance: a grid barrier timed out");
+    if (err & H4_ERRBIT_NONFINITE) return efail(H4_ERR_NONFINITE, "h4_ens_advance: non-finite state in a system");
+    if (err & H4_ERRBIT_STEPCAP) return efail(H4_ERR_STATE, "h4_ens_advance: launch bound reached");
+    return H4_OK;
+}
+
+int h4_ens_energy(h4_ens_handle E, double *ekin, double *epot) {
+    if (!E) return efail(H4_ERR_ARG, "null handle");
+    k_ens_energy_pairs<<<E->num_sms * 8, THREADS, 0, E->stream>>>(E->d);
+    k_ens_energy_sum<<<std::min(E->nsys, 4096), THREADS, 0, E->stream>>>(E->d);
+    E->launches += 2;
+    ENS_TRY(cudaGetLastError(), "h4_ens_energy launch");
+    std::vector<double> en(2 * (size_t)E->nsys);
+    ENS_TRY(cudaMemcpyAsync(en.data(), E->d.energy, sizeof(double) * en.size(), cudaMemcpyDeviceToHost, E->stream), "energy");
+    ENS_TRY(cudaStreamSynchronize(E->stream), "energy");
+    for (int c = 0; c < E->nsys; c++) {
+        if (ekin) ekin[c] = en[2 * c];
+        if (epot) epot[c] = en[2 * c + 1];
+    }
+    return H4_OK;
+}
+
+int h4_ens_download(h4_ens_handle E, h4_double4 *r, h4_double4 *v, h4_forces *f, double *t, double *dt) {
+    if (!E) return efail(H4_ERR_ARG, "null handle");
+    const size_t N = E->total;
+    cudaStream_t s = E->stream;
+    if (r) ENS_TRY(cudaMemcpyAsync(r, E->d.r, 32 * N, cudaMemcpyDeviceToHost, s), "download r");
+    if (v) ENS_TRY(cudaMemcpyAsync(v, E->d.v, 32 * N, cudaMemcpyDeviceToHost, s), "download v");
+    if (f) ENS_TRY(cudaMemcpyAsync(f, E->d.f, 48 * N, cudaMemcpyDeviceToHost, s), "download f");
+    if (t) ENS_TRY(cudaMemcpyAsync(t, E->d.t, 8 * N, cudaMemcpyDeviceToHost, s), "download t");
+    if (dt) ENS_TRY(cudaMemcpyAsync(dt, E->d.dt, 8 * N, cudaMemcpyDeviceToHost, s), "download dt");
+    ENS_TRY(cudaStreamSynchronize(s), "download");
+    return H4_OK;
+}
+
+int h4_ens_system_stats(h4_ens_handle E, double *itime, double *atime, unsigned long long *steps,
+                        unsigned long long *psteps, unsigned long long *inter) {
+    if (!E) return efail(H4_ERR_ARG, "null handle");
+    int st = pull_systems(E);
+    if (st) return st;
+    for (int c = 0; c < E->nsys; c++) {
+        const System &S = E->host_sys[c];
+        if (itime) itime[c] = S.itime;
+        if (atime) atime[c] = S.atime;
+        if (steps) steps[c] = S.steps;
+        if (psteps) psteps[c] = S.psteps;
+        if (inter) inter[c] = S.inter;
+    }
+    return H4_OK;
+}
+
+int h4_ens_tune_force(h4_ens_handle E, unsigned int nact, unsigned int ig, unsigned int chunk, float *ms) {
+    if (!E || !ms) return efail(H4_ERR_ARG, "null argument");
+    if (nact < 1) return efail(H4_ERR_ARG, "nact must be >= 1");
+    if (ig != 1 && ig != 2 && ig != 4) return efail(H4_ERR_ARG, "ig must be 1, 2 or 4");
+    std::vector<unsigned> tig(NB_N * NB_A, ig), tch(NB_N * NB_A, chunk);
+    int st = h4_ens_set_tuning(E, tig.data(), tch.data());
+    if (st) return st;
+    if ((st = pull_systems(E))) return st;
+    for (auto &S : E->host_sys) S.done = 0;
+    ENS_TRY(cudaMemcpyAsync(E->d.sys, E->host_sys.data(), sizeof(System) * E->nsys, cudaMemcpyHostToDevice, E->stream), "systems");
+    ENS_TRY(cudaMemcpyAsync(E->d.forced_nact, &nact, 4, cudaMemcpyHostToDevice, E->stream), "forced nact");
+    cudaEventRecord(E->e0, E->stream);
+    ENS_TRY(launch_persistent(E, E->stream, 1, 0, 1), "tune launch");
+    cudaEventRecord(E->e1, E->stream);
+    E->launches += 1;
+    const unsigned zero = 0;
+    ENS_TRY(cudaMemcpyAsync(E->d.forced_nact, &zero, 4, cudaMemcpyHostToDevice, E->stream), "forced nact");
+    ENS_TRY(cudaStreamSynchronize(E->stream), "tune");
+    cudaEventElapsedTime(ms, E->e0, E->e1);
+    unsigned err = 0;
+    ENS_TRY(cudaMemcpy(&err, E->d.err, 4, cudaMemcpyDeviceToHost), "error word");
+    if (err) return efail(H4_ERR_CUDA, "h4_ens_tune_force: device error bits " + std::to_string(err));
+    return H4_OK;
+}
+
+int h4_ens_timings(h4_ens_handle E, float *advance_ms, unsigned long long *kernel_launches) {
+    if (!E) return efail(H4_ERR_ARG, "null handle");
+    if (advance_ms) *advance_ms = E->last_ms;
+    if (kernel_launches) *kernel_launches = E->launches;
+    return H4_OK;
+}
+
+}  // extern "C"

@@ -26,6 +26,7 @@
 // Work items are handed out through an atomic counter in the control block
 // (reset by the active-set kernel of the step).
 #include "h4_internal.cuh"
+#include "h4_pair.cuh"
 
 namespace h4 {
 namespace {
@@ -33,82 +34,6 @@ namespace {
 constexpr int WARPS = 4;        // warps per block
 constexpr int IG = 4;           // active particles per work item
 constexpr int ITEMS_PER_WARP = 12;
-
-__device__ __forceinline__ double rsqrt_approx(double x) {
-    double y;
-    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    return y;
-}
-
-// 1/sqrt(x): hardware seed + one cubic Householder step.
-__device__ __forceinline__ double rsqrt_refined(double x) {
-    const double y0 = rsqrt_approx(x);
-    const double e = fma(-x, y0 * y0, 1.0);
-    const double c = fma(e, 0.375, 0.5);
-    return fma(y0 * e, c, y0);
-}
-
-template <int NI>
-__device__ __forceinline__ void force_item(const H4Dev &d, unsigned nact, unsigned k0,
-                                           int j_begin, int j_end, unsigned split, unsigned s,
-                                           int lane) {
-    double xi[NI], yi[NI], zi[NI], vxi[NI], vyi[NI], vzi[NI];
-    unsigned idx[NI];
-    double acc[NI][6];
-#pragma unroll
-    for (int q = 0; q < NI; q++) {
-        idx[q] = d.move[k0 + q];
-        const dbl4 p = d.pr[idx[q]], v = d.pv[idx[q]];
-        xi[q] = p.x; yi[q] = p.y; zi[q] = p.z;
-        vxi[q] = v.x; vyi[q] = v.y; vzi[q] = v.z;
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc[q][c] = 0.0;
-    }
-    const double e2 = d.e2;
-    for (int j = j_begin + lane; j < j_end; j += 32) {
-        const dbl4 pj = d.pr[j], vj = d.pv[j];
-#pragma unroll
-        for (int q = 0; q < NI; q++) {
-            const double dx = pj.x - xi[q], dy = pj.y - yi[q], dz = pj.z - zi[q];
-            const double dvx = vj.x - vxi[q], dvy = vj.y - vyi[q], dvz = vj.z - vzi[q];
-            double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, e2)));
-            double m = pj.w;
-            const bool self = (unsigned)j == idx[q];   // the reference skips i == j
-            r2 = self ? 1.0 : r2;
-            m = self ? 0.0 : m;
-            const double rinv = rsqrt_refined(r2);
-            const double r2inv = rinv * rinv;
-            const double A = (m * rinv) * r2inv;
-            const double rv = fma(dx, dvx, fma(dy, dvy, dz * dvz));
-            const double eta = rv * (-3.0 * r2inv);
-            acc[q][0] = fma(A, dx, acc[q][0]);
-            acc[q][1] = fma(A, dy, acc[q][1]);
-            acc[q][2] = fma(A, dz, acc[q][2]);
-            acc[q][3] = fma(A, fma(eta, dx, dvx), acc[q][3]);
-            acc[q][4] = fma(A, fma(eta, dy, dvy), acc[q][4]);
-            acc[q][5] = fma(A, fma(eta, dz, dvz), acc[q][5]);
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < NI; q++) {
-#pragma unroll
-        for (int c = 0; c < 6; c++) {
-            double a = acc[q][c];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-            acc[q][c] = a;
-        }
-    }
-    if (lane == 0) {
-        double *p = d.part + (size_t)s * 6 * nact;
-#pragma unroll
-        for (int q = 0; q < NI; q++) {
-#pragma unroll
-            for (int c = 0; c < 6; c++) p[(size_t)c * nact + k0 + q] = acc[q][c];
-        }
-    }
-    (void)split;
-}
 
 __global__ void __launch_bounds__(WARPS * 32) k_force_fp64(H4Dev d) {
     const unsigned nact = d.ctrl->nact;
@@ -143,12 +68,16 @@ __global__ void __launch_bounds__(WARPS * 32) k_force_fp64(H4Dev d) {
         const int j_end = min(d.n, j_begin + chunk);
         const unsigned k0 = g * IG;
         const unsigned cnt = min((unsigned)IG, nact - k0);
+        double *part_s = d.part + (size_t)s * 6 * nact;
         if (cnt == 4) {
-            force_item<4>(d, nact, k0, j_begin, j_end, split, s, lane);
+            pair::fp64_warp_item<4>(d.pr, d.pv, d.move, nact, k0, j_begin, j_end, d.e2, part_s, lane);
         } else {
             unsigned k = k0;
-            if (cnt >= 2) { force_item<2>(d, nact, k, j_begin, j_end, split, s, lane); k += 2; }
-            if (cnt & 1) force_item<1>(d, nact, k, j_begin, j_end, split, s, lane);
+            if (cnt >= 2) {
+                pair::fp64_warp_item<2>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
+                k += 2;
+            }
+            if (cnt & 1) pair::fp64_warp_item<1>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
         }
     }
 }
@@ -161,31 +90,8 @@ __global__ void __launch_bounds__(128) k_force_exact(H4Dev d) {
     const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
     if (blockIdx.x == 0 && threadIdx.x == 0) d.ctrl->force_split = 1;
     if (k >= nact) return;
-    const unsigned i = d.move[k];
-    const dbl4 pi = d.pr[i], vi = d.pv[i];
-    double f[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    const double e2 = d.e2;
-    for (int j = 0; j < d.n; j++) {
-        if ((unsigned)j == i) continue;
-        const dbl4 pj = d.pr[j], vj = d.pv[j];
-        const double rx = __dadd_rn(pj.x, -pi.x), ry = __dadd_rn(pj.y, -pi.y), rz = __dadd_rn(pj.z, -pi.z);
-        const double vx = __dadd_rn(vj.x, -vi.x), vy = __dadd_rn(vj.y, -vi.y), vz = __dadd_rn(vj.z, -vi.z);
-        const double r2 = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz)), e2);
-        const double rinv = __ddiv_rn(1.0, __dsqrt_rn(r2));
-        const double r2inv = __dmul_rn(rinv, rinv);
-        const double r3inv = __dmul_rn(r2inv, rinv);
-        const double r5inv = __dmul_rn(r2inv, r3inv);
-        const double mr3inv = __dmul_rn(r3inv, pj.w);
-        const double mr5inv = __dmul_rn(r5inv, pj.w);
-        const double rv = __dadd_rn(__dadd_rn(__dmul_rn(rx, vx), __dmul_rn(ry, vy)), __dmul_rn(rz, vz));
-        const double rv3 = __dmul_rn(3.0, rv);
-        f[0] = __dadd_rn(f[0], __dmul_rn(rx, mr3inv));
-        f[1] = __dadd_rn(f[1], __dmul_rn(ry, mr3inv));
-        f[2] = __dadd_rn(f[2], __dmul_rn(rz, mr3inv));
-        f[3] = __dadd_rn(f[3], __dadd_rn(__dmul_rn(vx, mr3inv), -__dmul_rn(__dmul_rn(rv3, rx), mr5inv)));
-        f[4] = __dadd_rn(f[4], __dadd_rn(__dmul_rn(vy, mr3inv), -__dmul_rn(__dmul_rn(rv3, ry), mr5inv)));
-        f[5] = __dadd_rn(f[5], __dadd_rn(__dmul_rn(vz, mr3inv), -__dmul_rn(__dmul_rn(rv3, rz), mr5inv)));
-    }
+    double f[6];
+    pair::exact_sum(d.pr, d.pv, d.n, d.move[k], d.e2, f);
 #pragma unroll
     for (int c = 0; c < 6; c++) d.part[(size_t)c * nact + k] = f[c];
 }

@@ -29,6 +29,7 @@
 #include <stdint.h>
 
 #include "h4_internal.cuh"
+#include "h4_pair.cuh"
 
 namespace h4 {
 namespace {
@@ -77,53 +78,12 @@ __device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned
         : "memory");
 }
 
-__device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
-    const float y = x - c;
-    const float t = s + y;
-    c = (t - s) - y;
-    s = t;
-}
-
-struct IParticle {
-    float xh, yh, zh, xl, yl, zl, vx, vy, vz;
-};
+using pair::IParticle;
+using pair::kahan_add;
+using pair::pair_mixed;
 
 __device__ __forceinline__ IParticle load_i(const H4Dev &d, unsigned i) {
-    const float4 a = d.jf0[i], b = d.jf1[i], c = d.jf2[i];
-    IParticle p;
-    p.xh = a.x; p.yh = a.y; p.zh = a.z;
-    p.xl = b.x; p.yl = b.y; p.zl = b.z;
-    p.vx = c.x; p.vy = c.y; p.vz = c.z;
-    return p;
-}
-
-// One pair, FP32 after the double-single difference.  `sum` gets the six
-// terms (acc, jerk).  With e2 = 0 the self term is masked explicitly; with
-// e2 > 0 it is an exact zero (dr = dv = 0).
-template <bool MASK_SELF>
-__device__ __forceinline__ void pair_mixed(const IParticle &p, float4 j0, float4 j1, float4 j2, float e2,
-                                           bool self, float sum[6]) {
-    const float dx = (j0.x - p.xh) + (j1.x - p.xl);
-    const float dy = (j0.y - p.yh) + (j1.y - p.yl);
-    const float dz = (j0.z - p.zh) + (j1.z - p.zl);
-    const float dvx = j2.x - p.vx, dvy = j2.y - p.vy, dvz = j2.z - p.vz;
-    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e2)));
-    float m = j0.w;
-    if (MASK_SELF) {
-        r2 = self ? 1.0f : r2;
-        m = self ? 0.0f : m;
-    }
-    const float rinv = rsqrtf(r2);
-    const float r2inv = rinv * rinv;
-    const float A = (m * rinv) * r2inv;
-    const float rv = fmaf(dx, dvx, fmaf(dy, dvy, dz * dvz));
-    const float eta = rv * (-3.0f * r2inv);
-    sum[0] = fmaf(A, dx, sum[0]);
-    sum[1] = fmaf(A, dy, sum[1]);
-    sum[2] = fmaf(A, dz, sum[2]);
-    sum[3] = fmaf(A, fmaf(eta, dx, dvx), sum[3]);
-    sum[4] = fmaf(A, fmaf(eta, dy, dvy), sum[4]);
-    sum[5] = fmaf(A, fmaf(eta, dz, dvz), sum[5]);
+    return pair::load_i(d.jf0, d.jf1, d.jf2, i);
 }
 
 struct MixedSplit {
@@ -275,48 +235,6 @@ __device__ __forceinline__ MixedSplit warp_split(const H4Dev &d, unsigned nact, 
     return s;
 }
 
-template <int NI, bool MASK_SELF>
-__device__ __forceinline__ void warp_item(const H4Dev &d, unsigned nact, unsigned k0, int j_begin, int j_end,
-                                          unsigned s, int lane, float e2) {
-    IParticle ip[NI];
-    unsigned idx[NI];
-    float S[NI][6], C[NI][6];
-#pragma unroll
-    for (int q = 0; q < NI; q++) {
-        idx[q] = d.move[k0 + q];
-        ip[q] = load_i(d, idx[q]);
-#pragma unroll
-        for (int c = 0; c < 6; c++) { S[q][c] = 0.f; C[q][c] = 0.f; }
-    }
-    for (int jb = j_begin; jb < j_end; jb += 32 * 16) {
-        float part[NI][6];
-#pragma unroll
-        for (int q = 0; q < NI; q++)
-#pragma unroll
-            for (int c = 0; c < 6; c++) part[q][c] = 0.f;
-        const int jl = min(j_end, jb + 32 * 16);
-        for (int j = jb + lane; j < jl; j += 32) {
-            const float4 j0 = d.jf0[j], j1 = d.jf1[j], j2 = d.jf2[j];
-#pragma unroll
-            for (int q = 0; q < NI; q++) pair_mixed<MASK_SELF>(ip[q], j0, j1, j2, e2, (unsigned)j == idx[q], part[q]);
-        }
-#pragma unroll
-        for (int q = 0; q < NI; q++)
-#pragma unroll
-            for (int c = 0; c < 6; c++) kahan_add(S[q][c], C[q][c], part[q][c]);
-    }
-#pragma unroll
-    for (int q = 0; q < NI; q++) {
-#pragma unroll
-        for (int c = 0; c < 6; c++) {
-            double a = (double)S[q][c] - (double)C[q][c];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-            if (lane == 0) d.part[(size_t)s * 6 * nact + (size_t)c * nact + k0 + q] = a;
-        }
-    }
-}
-
 template <bool MASK_SELF>
 __global__ void __launch_bounds__(WARPS_W * 32) k_force_mixed_warp(H4Dev d, unsigned threshold) {
     const unsigned nact = d.ctrl->nact;
@@ -339,12 +257,19 @@ __global__ void __launch_bounds__(WARPS_W * 32) k_force_mixed_warp(H4Dev d, unsi
         const int j_end = min(d.n, j_begin + sp.chunk);
         const unsigned k0 = g * IGW;
         const unsigned cnt = min((unsigned)IGW, nact - k0);
+        double *part_s = d.part + (size_t)s * 6 * nact;
         if (cnt == 4) {
-            warp_item<4, MASK_SELF>(d, nact, k0, j_begin, j_end, s, lane, e2);
+            pair::mixed_warp_item<4, MASK_SELF>(d.jf0, d.jf1, d.jf2, d.move, nact, k0, j_begin, j_end, e2, part_s, lane);
         } else {
             unsigned k = k0;
-            if (cnt >= 2) { warp_item<2, MASK_SELF>(d, nact, k, j_begin, j_end, s, lane, e2); k += 2; }
-            if (cnt & 1) warp_item<1, MASK_SELF>(d, nact, k, j_begin, j_end, s, lane, e2);
+            if (cnt >= 2) {
+                pair::mixed_warp_item<2, MASK_SELF>(d.jf0, d.jf1, d.jf2, d.move, nact, k, j_begin, j_end, e2, part_s,
+                                                    lane);
+                k += 2;
+            }
+            if (cnt & 1)
+                pair::mixed_warp_item<1, MASK_SELF>(d.jf0, d.jf1, d.jf2, d.move, nact, k, j_begin, j_end, e2, part_s,
+                                                    lane);
         }
     }
 }

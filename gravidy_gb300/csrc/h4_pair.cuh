@@ -1,0 +1,213 @@
+// Pair arithmetic and warp work items of the force sum, shared by the
+// single-system force kernels and the ensemble kernel.
+//
+// A warp item is (up to 4 active particles, one j range): the 32 lanes take
+// interleaved j, every lane keeps the sums of all the item's particles, and a
+// fixed shuffle tree combines the lanes at the end (deterministic).  Results
+// go to part_s[c * nact + k] (component c of active particle k, for this
+// j-chunk).  Indices in `move` and j are relative to the arrays passed.
+#pragma once
+#include "h4_internal.cuh"
+
+namespace h4 {
+namespace pair {
+
+// 1/sqrt(x) in FP64: hardware reciprocal-square-root approximation
+// (rsqrt.approx.f64) refined by one cubic Householder step,
+// y = y0 (1 + e/2 + 3e^2/8) with e = 1 - x y0^2.
+__device__ __forceinline__ double rsqrt_refined(double x) {
+    double y0;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y0) : "d"(x));
+    const double e = fma(-x, y0 * y0, 1.0);
+    return fma(y0 * e, fma(e, 0.375, 0.5), y0);
+}
+
+// FP64 pair (Hermite4CPU::force_calculation, Hermite4CPU.cpp:55-82), written
+// as a = A dr, a1 = A (dv - 3 (dr.dv)/r^2 dr), A = m / r^3: 31 FP64
+// instructions.  The self pair (j == i) is skipped by a select, as the
+// reference skips it (Hermite4CPU.cpp:328).
+__device__ __forceinline__ void pair_fp64(double xi, double yi, double zi, double vxi, double vyi, double vzi,
+                                          const dbl4 &pj, const dbl4 &vj, double e2, bool self, double acc[6]) {
+    const double dx = pj.x - xi, dy = pj.y - yi, dz = pj.z - zi;
+    const double dvx = vj.x - vxi, dvy = vj.y - vyi, dvz = vj.z - vzi;
+    double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, e2)));
+    double m = pj.w;
+    r2 = self ? 1.0 : r2;
+    m = self ? 0.0 : m;
+    const double rinv = rsqrt_refined(r2);
+    const double r2inv = rinv * rinv;
+    const double A = (m * rinv) * r2inv;
+    const double rv = fma(dx, dvx, fma(dy, dvy, dz * dvz));
+    const double eta = rv * (-3.0 * r2inv);
+    acc[0] = fma(A, dx, acc[0]);
+    acc[1] = fma(A, dy, acc[1]);
+    acc[2] = fma(A, dz, acc[2]);
+    acc[3] = fma(A, fma(eta, dx, dvx), acc[3]);
+    acc[4] = fma(A, fma(eta, dy, dvy), acc[4]);
+    acc[5] = fma(A, fma(eta, dz, dvz), acc[5]);
+}
+
+template <int NI>
+__device__ __forceinline__ void fp64_warp_item(const dbl4 *__restrict__ pr, const dbl4 *__restrict__ pv,
+                                               const unsigned *__restrict__ move, unsigned nact, unsigned k0,
+                                               int j_begin, int j_end, double e2, double *part_s, int lane) {
+    double xi[NI], yi[NI], zi[NI], vxi[NI], vyi[NI], vzi[NI];
+    unsigned idx[NI];
+    double acc[NI][6];
+#pragma unroll
+    for (int q = 0; q < NI; q++) {
+        idx[q] = move[k0 + q];
+        const dbl4 p = pr[idx[q]], v = pv[idx[q]];
+        xi[q] = p.x; yi[q] = p.y; zi[q] = p.z;
+        vxi[q] = v.x; vyi[q] = v.y; vzi[q] = v.z;
+#pragma unroll
+        for (int c = 0; c < 6; c++) acc[q][c] = 0.0;
+    }
+    for (int j = j_begin + lane; j < j_end; j += 32) {
+        const dbl4 pj = pr[j], vj = pv[j];
+#pragma unroll
+        for (int q = 0; q < NI; q++)
+            pair_fp64(xi[q], yi[q], zi[q], vxi[q], vyi[q], vzi[q], pj, vj, e2, (unsigned)j == idx[q], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < NI; q++) {
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            double a = acc[q][c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            if (lane == 0) part_s[(size_t)c * nact + k0 + q] = a;
+        }
+    }
+}
+
+// Bit-identical restatement of the reference's per-particle sum (one thread,
+// j ascending, the reference's operation order, IEEE sqrt and division).
+__device__ __forceinline__ void exact_sum(const dbl4 *__restrict__ pr, const dbl4 *__restrict__ pv, int n,
+                                          unsigned i, double e2, double f[6]) {
+    const dbl4 pi = pr[i], vi = pv[i];
+#pragma unroll
+    for (int c = 0; c < 6; c++) f[c] = 0.0;
+    for (int j = 0; j < n; j++) {
+        if ((unsigned)j == i) continue;
+        const dbl4 pj = pr[j], vj = pv[j];
+        const double rx = __dadd_rn(pj.x, -pi.x), ry = __dadd_rn(pj.y, -pi.y), rz = __dadd_rn(pj.z, -pi.z);
+        const double vx = __dadd_rn(vj.x, -vi.x), vy = __dadd_rn(vj.y, -vi.y), vz = __dadd_rn(vj.z, -vi.z);
+        const double r2 =
+            __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz)), e2);
+        const double rinv = __ddiv_rn(1.0, __dsqrt_rn(r2));
+        const double r2inv = __dmul_rn(rinv, rinv);
+        const double r3inv = __dmul_rn(r2inv, rinv);
+        const double r5inv = __dmul_rn(r2inv, r3inv);
+        const double mr3inv = __dmul_rn(r3inv, pj.w);
+        const double mr5inv = __dmul_rn(r5inv, pj.w);
+        const double rv = __dadd_rn(__dadd_rn(__dmul_rn(rx, vx), __dmul_rn(ry, vy)), __dmul_rn(rz, vz));
+        const double rv3 = __dmul_rn(3.0, rv);
+        f[0] = __dadd_rn(f[0], __dmul_rn(rx, mr3inv));
+        f[1] = __dadd_rn(f[1], __dmul_rn(ry, mr3inv));
+        f[2] = __dadd_rn(f[2], __dmul_rn(rz, mr3inv));
+        f[3] = __dadd_rn(f[3], __dadd_rn(__dmul_rn(vx, mr3inv), -__dmul_rn(__dmul_rn(rv3, rx), mr5inv)));
+        f[4] = __dadd_rn(f[4], __dadd_rn(__dmul_rn(vy, mr3inv), -__dmul_rn(__dmul_rn(rv3, ry), mr5inv)));
+        f[5] = __dadd_rn(f[5], __dadd_rn(__dmul_rn(vz, mr3inv), -__dmul_rn(__dmul_rn(rv3, rz), mr5inv)));
+    }
+}
+
+// ---- mixed precision ----------------------------------------------------------
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+struct IParticle {
+    float xh, yh, zh, xl, yl, zl, vx, vy, vz;
+};
+
+__device__ __forceinline__ IParticle load_i(const float4 *jf0, const float4 *jf1, const float4 *jf2, unsigned i) {
+    const float4 a = jf0[i], b = jf1[i], c = jf2[i];
+    IParticle p;
+    p.xh = a.x; p.yh = a.y; p.zh = a.z;
+    p.xl = b.x; p.yl = b.y; p.zl = b.z;
+    p.vx = c.x; p.vy = c.y; p.vz = c.z;
+    return p;
+}
+
+// One pair, FP32 after the double-single difference of the positions.  With
+// e2 = 0 the self term is masked explicitly; with e2 > 0 it is an exact zero
+// (dr = dv = 0).
+template <bool MASK_SELF>
+__device__ __forceinline__ void pair_mixed(const IParticle &p, float4 j0, float4 j1, float4 j2, float e2,
+                                           bool self, float sum[6]) {
+    const float dx = (j0.x - p.xh) + (j1.x - p.xl);
+    const float dy = (j0.y - p.yh) + (j1.y - p.yl);
+    const float dz = (j0.z - p.zh) + (j1.z - p.zl);
+    const float dvx = j2.x - p.vx, dvy = j2.y - p.vy, dvz = j2.z - p.vz;
+    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e2)));
+    float m = j0.w;
+    if (MASK_SELF) {
+        r2 = self ? 1.0f : r2;
+        m = self ? 0.0f : m;
+    }
+    const float rinv = rsqrtf(r2);
+    const float r2inv = rinv * rinv;
+    const float A = (m * rinv) * r2inv;
+    const float rv = fmaf(dx, dvx, fmaf(dy, dvy, dz * dvz));
+    const float eta = rv * (-3.0f * r2inv);
+    sum[0] = fmaf(A, dx, sum[0]);
+    sum[1] = fmaf(A, dy, sum[1]);
+    sum[2] = fmaf(A, dz, sum[2]);
+    sum[3] = fmaf(A, fmaf(eta, dx, dvx), sum[3]);
+    sum[4] = fmaf(A, fmaf(eta, dy, dvy), sum[4]);
+    sum[5] = fmaf(A, fmaf(eta, dz, dvz), sum[5]);
+}
+
+// Mixed warp item: FP32 lane sums over runs of 16 j, Kahan-compensated
+// across runs, FP64 shuffle tree across lanes.
+template <int NI, bool MASK_SELF>
+__device__ __forceinline__ void mixed_warp_item(const float4 *__restrict__ jf0, const float4 *__restrict__ jf1,
+                                                const float4 *__restrict__ jf2, const unsigned *__restrict__ move,
+                                                unsigned nact, unsigned k0, int j_begin, int j_end, float e2,
+                                                double *part_s, int lane) {
+    IParticle ip[NI];
+    unsigned idx[NI];
+    float S[NI][6], C[NI][6];
+#pragma unroll
+    for (int q = 0; q < NI; q++) {
+        idx[q] = move[k0 + q];
+        ip[q] = load_i(jf0, jf1, jf2, idx[q]);
+#pragma unroll
+        for (int c = 0; c < 6; c++) { S[q][c] = 0.f; C[q][c] = 0.f; }
+    }
+    for (int jb = j_begin; jb < j_end; jb += 32 * 16) {
+        float part[NI][6];
+#pragma unroll
+        for (int q = 0; q < NI; q++)
+#pragma unroll
+            for (int c = 0; c < 6; c++) part[q][c] = 0.f;
+        const int jl = min(j_end, jb + 32 * 16);
+        for (int j = jb + lane; j < jl; j += 32) {
+            const float4 j0 = jf0[j], j1 = jf1[j], j2 = jf2[j];
+#pragma unroll
+            for (int q = 0; q < NI; q++) pair_mixed<MASK_SELF>(ip[q], j0, j1, j2, e2, (unsigned)j == idx[q], part[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < NI; q++)
+#pragma unroll
+            for (int c = 0; c < 6; c++) kahan_add(S[q][c], C[q][c], part[q][c]);
+    }
+#pragma unroll
+    for (int q = 0; q < NI; q++) {
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            double a = (double)S[q][c] - (double)C[q][c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            if (lane == 0) part_s[(size_t)c * nact + k0 + q] = a;
+        }
+    }
+}
+
+}  // namespace pair
+}  // namespace h4

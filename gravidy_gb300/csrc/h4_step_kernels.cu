@@ -8,35 +8,20 @@
 // the reference build (g++ on x86-64) never does; with the intrinsics the
 // predictor, corrector, timestep and active-set results are bit-identical to
 // the reference's for identical inputs.
+#include "h4_exact.cuh"
 #include "h4_internal.cuh"
 
 namespace h4 {
 namespace {
 
-__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double sub(double a, double b) { return __dadd_rn(a, -b); }
-__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
-
-__device__ __forceinline__ double bits_to_double(unsigned long long b) {
-    return __longlong_as_double((long long)b);
-}
-__device__ __forceinline__ unsigned long long double_to_bits(double x) {
-    return (unsigned long long)__double_as_longlong(x);
-}
-constexpr unsigned long long INF_BITS = 0x7FF0000000000000ull;
-
-// NbodyUtils::get_magnitude (NbodyUtils.cpp:331-334): sqrt(x*x + y*y + z*z).
-__device__ __forceinline__ double magnitude(double x, double y, double z) {
-    return __dsqrt_rn(add(add(mul(x, x), mul(y, y)), mul(z, z)));
-}
-
-// Active test of Hermite4::find_particles_to_move (Hermite4.cpp:74-76):
-// |ITIME - (t + dt)| < 2 * DBL_EPSILON.
-__device__ __forceinline__ bool is_active(double itime, double t, double dt) {
-    double tmp = add(t, dt);
-    return fabs(sub(itime, tmp)) < 4.440892098500626e-16;
-}
+using exact::add;
+using exact::bits_to_double;
+using exact::double_to_bits;
+using exact::dvd;
+using exact::INF_BITS;
+using exact::is_active;
+using exact::mul;
+using exact::sub;
 
 // Block-wide exclusive scan of one unsigned per thread (FLAG_THREADS threads).
 __device__ unsigned block_exclusive_scan(unsigned x) {
@@ -84,21 +69,10 @@ __device__ unsigned block_sum(unsigned x) {
     return s;
 }
 
-// Double-single split of a double: hi = fl32(x), lo = fl32(x - hi).
-__device__ __forceinline__ void ds_split(double x, float &hi, float &lo) {
-    hi = __double2float_rn(x);
-    lo = __double2float_rn(__dadd_rn(x, -(double)hi));
-}
-
 // Packed FP32 j data of the mixed kernels, from predicted position/velocity.
 __device__ __forceinline__ void write_jf(const H4Dev &d, int i, const dbl4 &pr, const dbl4 &pv) {
     float4 a, b, c;
-    ds_split(pr.x, a.x, b.x);
-    ds_split(pr.y, a.y, b.y);
-    ds_split(pr.z, a.z, b.z);
-    a.w = (float)pr.w;
-    b.w = 0.f;
-    c = make_float4((float)pv.x, (float)pv.y, (float)pv.z, 0.f);
+    exact::pack_jf(pr, pv, a, b, c);
     d.jf0[i] = a;
     d.jf1[i] = b;
     d.jf2[i] = c;
@@ -169,22 +143,8 @@ __global__ void __launch_bounds__(256) k_predict(H4Dev d, int host_itime, double
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     const double itime = host_itime ? itime_in : d.ctrl->itime;
-    const double dt = sub(itime, d.t[i]);
-    const double dt2 = mul(dt, dt);
-    const double dt3 = mul(dt2, dt);
-    const double dt2c = dvd(dt2, 2.0);
-    const double dt3c = dvd(dt3, 6.0);
-    const double *f = d.f + 6 * (size_t)i;
-    const dbl4 r = d.r[i], v = d.v[i];
     dbl4 pr, pv;
-    pr.x = add(add(add(mul(dt3c, f[3]), mul(dt2c, f[0])), mul(dt, v.x)), r.x);
-    pr.y = add(add(add(mul(dt3c, f[4]), mul(dt2c, f[1])), mul(dt, v.y)), r.y);
-    pr.z = add(add(add(mul(dt3c, f[5]), mul(dt2c, f[2])), mul(dt, v.z)), r.z);
-    pr.w = (double)(float)r.w;   // Predictor::m is a float (common.hpp:216)
-    pv.x = add(add(mul(dt2c, f[3]), mul(dt, f[0])), v.x);
-    pv.y = add(add(mul(dt2c, f[4]), mul(dt, f[1])), v.y);
-    pv.z = add(add(mul(dt2c, f[5]), mul(dt, f[2])), v.z);
-    pv.w = 0.0;
+    exact::predict(itime, d.t[i], d.f + 6 * (size_t)i, d.r[i], d.v[i], pr, pv);
     d.pr[i] = pr;
     d.pv[i] = pv;
     if (d.jf0) write_jf(d, i, pr, pv);
@@ -255,33 +215,6 @@ __global__ void k_reduce_forces(H4Dev d, int save_old) {
     }
 }
 
-// NbodyUtils::normalize_dt (NbodyUtils.cpp:371-424).
-__device__ double normalize_dt(const H4Dev &d, double new_dt, double old_dt, double t) {
-    const double o8 = dvd(old_dt, 8.0), o4 = dvd(old_dt, 4.0), o2 = dvd(old_dt, 2.0);
-    const double o2x = mul(old_dt, 2.0), x2o = mul(2.0, old_dt);
-    if (new_dt <= o8) {
-        new_dt = 1.1920928955078125e-07;  // D_TIME_MIN (common.hpp:122), not the handle's bound
-    } else if (o8 < new_dt && new_dt <= o4) {
-        new_dt = o8;
-    } else if (o4 < new_dt && new_dt <= o2) {
-        new_dt = o4;
-    } else if (o2 < new_dt && new_dt <= old_dt) {
-        new_dt = o2;
-    } else if (old_dt < new_dt && new_dt <= o2x) {
-        new_dt = old_dt;
-    } else if (x2o < new_dt) {
-        const double val = dvd(t, x2o);
-        new_dt = (ceil(val) == val) ? mul(2.0, old_dt) : old_dt;
-    } else {
-        new_dt = old_dt;
-    }
-    if (new_dt < d.dt_min)
-        new_dt = d.dt_min;
-    else if (new_dt > d.dt_max)
-        new_dt = d.dt_max;
-    return new_dt;
-}
-
 // ---- Hermite4CPU::correction_pos_vel (Hermite4CPU.cpp:370-411) --------------
 // with NbodyUtils::get_timestep_normal (NbodyUtils.cpp:337-365).
 __global__ void __launch_bounds__(128) k_correct(H4Dev d, int host_itime, double itime_in, int fused_reduce) {
@@ -300,53 +233,17 @@ __global__ void __launch_bounds__(128) k_correct(H4Dev d, int host_itime, double
 #pragma unroll
             for (int c = 0; c < 6; c++) { f[c] = fp[c]; o[c] = op[c]; }
         }
-        const dbl4 p = d.pr[i], pv = d.pv[i];
-        const double dt1 = d.dt[i];
-        const double dt2 = mul(dt1, dt1);
-        const double dt3 = mul(dt2, dt1);
-        const double dt4 = mul(dt2, dt2);
-        const double dt5 = mul(dt4, dt1);
-        double a2[3], a3[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            // (-6 (a0 - a1) - dt (4 j0 + 2 j1)) / dt^2
-            a2[c] = dvd(sub(mul(-6.0, sub(o[c], f[c])),
-                            mul(dt1, add(mul(4.0, o[3 + c]), mul(2.0, f[3 + c])))), dt2);
-            // (12 (a0 - a1) + 6 dt (j0 + j1)) / dt^3
-            a3[c] = dvd(add(mul(12.0, sub(o[c], f[c])),
-                            mul(mul(6.0, dt1), add(o[3 + c], f[3 + c]))), dt3);
-        }
-        const double c24 = dvd(dt4, 24.0), c120 = dvd(dt5, 120.0), c6 = dvd(dt3, 6.0);
         dbl4 r = d.r[i], v = d.v[i];
-        r.x = add(add(p.x, mul(c24, a2[0])), mul(c120, a3[0]));
-        r.y = add(add(p.y, mul(c24, a2[1])), mul(c120, a3[1]));
-        r.z = add(add(p.z, mul(c24, a2[2])), mul(c120, a3[2]));
-        v.x = add(add(pv.x, mul(c6, a2[0])), mul(c24, a3[0]));
-        v.y = add(add(pv.y, mul(c6, a2[1])), mul(c24, a3[1]));
-        v.z = add(add(pv.z, mul(c6, a2[2])), mul(c24, a3[2]));
+        double a2[3], a3[3], ndt;
+        const bool ok = exact::correct(itime, d.eta, d.dt_min, d.dt_max, f, o, d.pr[i], d.pv[i], d.dt[i], r, v,
+                                       a2, a3, ndt);
         d.r[i] = r;
         d.v[i] = v;
 #pragma unroll
         for (int c = 0; c < 3; c++) { d.a2[3 * (size_t)i + c] = a2[c]; d.a3[3 * (size_t)i + c] = a3[c]; }
         d.t[i] = itime;
-
-        // get_timestep_normal, with the step's old dt as the reference uses it.
-        const double ax1 = add(a2[0], mul(dt1, a3[0]));
-        const double ay1 = add(a2[1], mul(dt1, a3[1]));
-        const double az1 = add(a2[2], mul(dt1, a3[2]));
-        const double abs_a1 = magnitude(f[0], f[1], f[2]);
-        const double abs_j1 = magnitude(f[3], f[4], f[5]);
-        const double abs_j12 = mul(abs_j1, abs_j1);
-        const double abs_a1_3 = magnitude(a3[0], a3[1], a3[2]);
-        const double abs_a1_2 = magnitude(ax1, ay1, az1);
-        const double abs_a1_22 = mul(abs_a1_2, abs_a1_2);
-        const double normal_dt = __dsqrt_rn(mul(d.eta, dvd(add(mul(abs_a1, abs_a1_2), abs_j12),
-                                                            add(mul(abs_j1, abs_a1_3), abs_a1_22))));
-        const double ndt = normalize_dt(d, normal_dt, dt1, itime);
         d.dt[i] = ndt;
-        if (!isfinite(r.x) || !isfinite(r.y) || !isfinite(r.z) || !isfinite(v.x) ||
-            !isfinite(v.y) || !isfinite(v.z))
-            atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_NONFINITE);
+        if (!ok) atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_NONFINITE);
     }
 }
 
@@ -368,29 +265,12 @@ __global__ void __launch_bounds__(256) k_next_time(H4Dev d) {
     }
 }
 
-// (int) of a double as x86-64 converts it (NaN and out-of-range -> INT_MIN);
-// the reference relies on that for particles without jerk (Hermite4.cpp:124).
-__device__ __forceinline__ int trunc_to_int_x86(double x) {
-    if (!(x > -2147483649.0 && x < 2147483648.0)) return INT_MIN;
-    return (int)x;
-}
-
 // ---- Hermite4::init_dt (Hermite4.cpp:108-140) -------------------------------
 __global__ void k_init_dt(H4Dev d, double eta, double itime) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double tmp = __longlong_as_double((long long)INF_BITS);
     if (i < d.n) {
-        const double *f = d.f + 6 * (size_t)i;
-        const double a2 = magnitude(f[0], f[1], f[2]);
-        const double j2 = magnitude(f[3], f[4], f[5]);
-        tmp = mul(eta, dvd(a2, j2));
-        // log(2.0), correctly rounded: 0x3FE62E42FEFA39EF
-        const int ex = trunc_to_int_x86(sub(ceil(dvd(log(tmp), 0x1.62e42fefa39efp-1)), 1.0));
-        tmp = ldexp(1.0, ex);   // pow(2, ex): exact
-        if (tmp < d.dt_min)
-            tmp = d.dt_min;
-        else if (tmp > d.dt_max)
-            tmp = d.dt_max;
+        tmp = exact::init_dt(d.f + 6 * (size_t)i, eta, d.dt_min, d.dt_max);
         d.dt[i] = tmp;
         d.t[i] = itime;
     }

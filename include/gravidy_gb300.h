@@ -164,6 +164,54 @@ int h4_download_predicted(h4_handle h, h4_double4 *pr, h4_double4 *pv);
 int h4_forces_for(h4_handle h, const h4_double4 *pr, const h4_double4 *pv,
                   unsigned int nact, const unsigned int *move, h4_forces *out);
 
+/* ---- Batched ensemble ------------------------------------------------------
+ * Many independent systems (e.g. star clusters of uneven N), each with its own
+ * block time and active set, advanced together: one persistent fused kernel
+ * per iteration does one block step of every unfinished system (active set +
+ * predictor, force sum from one work queue over all systems, corrector +
+ * timesteps + next time), replayed from a CUDA graph with a device-side while
+ * loop.  No counterpart in the reference, which integrates one system per
+ * process (src/gravidy.cpp:54-115); per system the arithmetic is that of the
+ * calls above.  Systems are stored back to back: system c owns particles
+ * [sum n[0..c), sum n[0..c]) of every concatenated array. */
+typedef struct h4_ensemble_s *h4_ens_handle;
+/* Tuning table: for (N bucket b, active-count bucket a) at index b*NB_A + a:
+ * particles per warp item (1, 2 or 4) and j-chunk length.  N buckets:
+ * <=512, <=1k, <=2k, <=4k, <=8k, larger; active buckets: 1, 2-3, 4-15,
+ * 16-63, 64-255, 256-1023, 1024-4095, >=4096. */
+#define H4_ENS_TUNE_NB_N 6
+#define H4_ENS_TUNE_NB_A 8
+const char *h4_ens_last_error(void);
+int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n,
+                  const double *e2, const float *eta, const h4_double4 *r,
+                  const h4_double4 *v, int mode);
+int h4_ens_destroy(h4_ens_handle e);
+int h4_ens_set_stream(h4_ens_handle e, void *stream);
+int h4_ens_set_tuning(h4_ens_handle e, const unsigned int *ig,
+                      const unsigned int *chunk);
+int h4_ens_set_dt_limits(h4_ens_handle e, double dt_min, double dt_max);
+/* init_acc_jrk + init_dt (ETA_S) of every system. */
+int h4_ens_init(h4_ens_handle e);
+/* Block steps until every system's block time reaches its t_end[c] (the
+ * reference's while (ITIME < integration_time) per system).
+ * stats: [0] block steps (all systems) in this call, [1] particle steps and
+ * [2] interactions since creation, [3] kernel iterations (launches). */
+int h4_ens_advance(h4_ens_handle e, const double *t_end, double stats[4]);
+/* Kinetic and unsoftened potential energy of every system. */
+int h4_ens_energy(h4_ens_handle e, double *ekin, double *epot);
+int h4_ens_download(h4_ens_handle e, h4_double4 *r, h4_double4 *v,
+                    h4_forces *f, double *t, double *dt);
+int h4_ens_system_stats(h4_ens_handle e, double *itime, double *atime,
+                        unsigned long long *steps, unsigned long long *psteps,
+                        unsigned long long *inter);
+/* Autotuner probe: the force phase alone with every system's first nact
+ * particles active (positions as stored), using (ig, chunk) everywhere;
+ * *ms = device time.  Leaves the integration state unchanged. */
+int h4_ens_tune_force(h4_ens_handle e, unsigned int nact, unsigned int ig,
+                      unsigned int chunk, float *ms);
+int h4_ens_timings(h4_ens_handle e, float *advance_ms,
+                   unsigned long long *kernel_launches);
+
 /* Force sum that allocates nothing.  No counterpart in the reference.
  *
  * For callers that cannot call cudaMalloc -- an application that hands all

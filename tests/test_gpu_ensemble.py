@@ -1,0 +1,126 @@
+"""Batched ensemble (persistent fused kernel + graph) against per-system runs.
+
+  * exact force mode: every system's final state is bit-identical to the
+    oracle's (the reference CPU path restated) after the same block steps;
+  * FP64 mode: same block-step counts and times as the single-system GPU
+    path, states within 1e-9 (FP64 forces differ only in summation order);
+  * mixed mode: |dE/E| of every system within 2x of its FP64 value (+1e-9).
+"""
+import numpy as np
+import pytest
+
+from gravidy_gb300 import Hermite4GPU, NbodySystem, ics
+from gravidy_gb300.ensemble import Ensemble
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [2, 33, 100, 257, 512, 1000, 1500]
+
+
+def _systems(sizes, seed0=100):
+    out = []
+    for k, n in enumerate(sizes):
+        imf = "salpeter" if k % 2 else "equal"
+        m, p, v = ics.plummer(n, seed0 + k, imf)
+        out.append((m, p, v, 0.01, 0.01))
+    return out
+
+
+def _oracle_run(sysdef, t_end):
+    m, p, v, soft, eta = sysdef
+    o = orc.Oracle(m, p, v, orc.e2_from_softening(soft), eta)
+    o.init_acc_jrk()
+    atime = o.init_dt(0.0, float(orc.ETA_S))
+    itime, steps = 0.0, 0
+    while itime < t_end:
+        _, itime, atime = o.block_step(itime, atime)
+        steps += 1
+    return o, steps, itime
+
+
+def test_ensemble_exact_mode_bit_identical_to_oracle():
+    systems = _systems(SIZES)
+    t_end = 0.0625
+    with Ensemble(systems, mode="exact") as E:
+        E.init()
+        E.advance(t_end)
+        st = E.download()
+        stats = E.stats()
+    for c, sd in enumerate(systems):
+        o, steps, itime = _oracle_run(sd, t_end)
+        sl = E.system_slice(c)
+        assert int(stats["steps"][c]) == steps and stats["itime"][c] == itime, c
+        assert np.array_equal(st["r"][sl], o.r), c
+        assert np.array_equal(st["v"][sl][:, :3], o.v[:, :3]), c
+        assert np.array_equal(st["f"][sl], o.f), c
+        assert np.array_equal(st["dt"][sl], o.dt) and np.array_equal(st["t"][sl], o.t), c
+
+
+def test_ensemble_fp64_matches_single_system_runs():
+    systems = _systems(SIZES, seed0=300)
+    t_end = 0.125
+    with Ensemble(systems, mode="fp64") as E:
+        E.init()
+        E.advance(t_end)
+        st = E.download()
+        stats = E.stats()
+        etot, _, _ = E.energy()
+    for c, (m, p, v, soft, eta) in enumerate(systems):
+        ns = NbodySystem(m, p, v, softening=soft, eta=eta)
+        with Hermite4GPU(ns) as g:
+            g.init_acc_jrk()
+            atime = g.init_dt(1.0e10, float(orc.ETA_S), 0.0)
+            itime, atime, steps, _, _, _ = g.advance(t_end, 1e30, atime)
+            s1 = g.download()
+            e1 = g.get_energy_gpu()
+        sl = E.system_slice(c)
+        assert int(stats["steps"][c]) == steps and stats["itime"][c] == itime, c
+        assert np.abs(st["r"][sl] - s1["r"]).max() < 1e-9, c
+        assert np.array_equal(st["dt"][sl], s1["dt"]), c
+        assert abs(etot[c] - e1) < 1e-12 * abs(e1), c
+
+
+def test_ensemble_mixed_energy_error_close_to_fp64():
+    systems = _systems([512, 1024, 2048, 700], seed0=500)
+    t_end = 0.25
+    res = {}
+    for mode in ("fp64", "mixed"):
+        with Ensemble(systems, mode=mode) as E:
+            E.init()
+            e0, _, _ = E.energy()
+            E.advance(t_end)
+            e1, _, _ = E.energy()
+        res[mode] = np.abs((e1 - e0) / e0)
+    print("dE/E fp64", res["fp64"], "mixed", res["mixed"])
+    assert np.all(res["mixed"] <= 2 * res["fp64"] + 1e-9)
+
+
+def test_ensemble_tune_probe_leaves_state_unchanged():
+    systems = _systems([600, 900, 1200], seed0=700)
+    with Ensemble(systems, mode="fp64") as E:
+        E.init()
+        E.advance(0.03125)
+        a = E.download()
+        sa = E.stats()
+        for ig in (1, 2, 4):
+            for chunk in (64, 512):
+                assert E.tune_force(100, ig, chunk) > 0.0
+        b = E.download()
+        sb = E.stats()
+        for k in a:
+            assert np.array_equal(a[k], b[k]), k
+        assert np.array_equal(sa["itime"], sb["itime"])
+        E.advance(0.0625)
+        assert np.all(E.stats()["itime"] >= 0.0625)
+
+
+def test_ensemble_energy_matches_oracle():
+    systems = _systems([2, 37, 300], seed0=900)
+    with Ensemble(systems, mode="fp64") as E:
+        etot, ek, ep = E.energy()
+    for c, (m, p, v, soft, eta) in enumerate(systems):
+        o = orc.Oracle(m, p, v, orc.e2_from_softening(soft), eta)
+        e, k, pp = o.energy()
+        assert abs(ek[c] - k) <= 1e-12 * abs(k)
+        assert abs(ep[c] - pp) <= 1e-12 * max(abs(pp), 1e-300)
