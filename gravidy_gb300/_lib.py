@@ -49,6 +49,7 @@ SIGNATURES = {
     "h4_forces_for": (_i, [_vp, _vp, _vp, _u, _vp, _vp]),
     "h4_last_timings": (_i, [_vp, C.POINTER(_f), C.POINTER(_f)]),
     "h4_kernel_launches": (_i, [_vp, C.POINTER(C.c_ulonglong)]),
+    "h4_nact_histogram": (_i, [_vp, _vp]),
     "h4_probe_peaks": (_i, [_pd, _pd]),
     "h4_forces_noalloc": (_i, [_u, _d, _vp, _vp, _u, _vp, _vp, _vp]),
     "h4_ens_last_error": (C.c_char_p, []),

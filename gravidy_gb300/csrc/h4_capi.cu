@@ -585,6 +585,14 @@ int h4_last_timings(h4_handle h, float *force_ms, float *advance_ms) {
     return H4_OK;
 }
 
+int h4_nact_histogram(h4_handle h, unsigned long long counts[32]) {
+    if (!h || !counts) return fail(H4_ERR_ARG, "null argument");
+    int st = sync_ctrl(h);
+    if (st) return st;
+    for (int k = 0; k < 32; k++) counts[k] = h->h_ctrl->nact_hist[k];
+    return H4_OK;
+}
+
 int h4_kernel_launches(h4_handle h, unsigned long long *count) {
     if (!h || !count) return fail(H4_ERR_ARG, "null argument");
     *count = h->launches;

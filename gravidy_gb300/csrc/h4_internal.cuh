@@ -35,6 +35,7 @@ struct H4Ctrl {
     unsigned long long psteps;     // sum of nact
     unsigned long long inter;      // sum of nact * n
     unsigned long long max_steps;  // hard bound on steps of one advance call
+    unsigned long long nact_hist[32]; // block steps by floor(log2(nact)), since creation
     int running;                   // 1 while the device loop continues
     int pad_;
 };

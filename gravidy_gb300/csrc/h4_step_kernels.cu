@@ -303,6 +303,7 @@ __global__ void k_advance_bookkeeping(H4Dev d, cudaGraphConditionalHandle cond, 
     const unsigned nact = c->nact;
     c->steps += 1;
     c->psteps += nact;
+    if (nact) c->nact_hist[31 - __clz(nact)] += 1;
     c->inter += (unsigned long long)nact * (unsigned long long)d.n;
     const double itime = c->itime;
     // Every step advances the block time by at least dt_min (times are

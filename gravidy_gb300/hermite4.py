@@ -258,6 +258,11 @@ class Hermite4GPU:
         _lib.check(self.L.h4_last_timings(self.h, C.byref(f), C.byref(a)))
         return f.value, a.value
 
+    def nact_histogram(self) -> np.ndarray:
+        out = np.zeros(32, dtype=np.uint64)
+        _lib.check(self.L.h4_nact_histogram(self.h, out.ctypes.data))
+        return out
+
     def kernel_launches(self) -> int:
         c = C.c_ulonglong()
         _lib.check(self.L.h4_kernel_launches(self.h, C.byref(c)))

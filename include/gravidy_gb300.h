@@ -243,6 +243,9 @@ const char *h4_forces_noalloc_error(void);
 /* Device time (ms) of the last force kernel launch and of the last
  * h4_advance call, measured with CUDA events on the handle's stream. */
 int h4_last_timings(h4_handle h, float *force_ms, float *advance_ms);
+/* Block steps run by h4_advance since creation, by active-set size:
+ * counts[k] = steps with 2^k <= nact < 2^(k+1). */
+int h4_nact_histogram(h4_handle h, unsigned long long counts[32]);
 /* Kernels launched by this handle since creation. */
 int h4_kernel_launches(h4_handle h, unsigned long long *count);
 
