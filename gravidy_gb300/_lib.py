@@ -46,6 +46,7 @@ SIGNATURES = {
     "h4_download": (_i, [_vp] + [_vp] * 9),
     "h4_upload": (_i, [_vp] + [_vp] * 6),
     "h4_download_predicted": (_i, [_vp, _vp, _vp]),
+    "h4_restore": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _d]),
     "h4_forces_for": (_i, [_vp, _vp, _vp, _u, _vp, _vp]),
     "h4_last_timings": (_i, [_vp, C.POINTER(_f), C.POINTER(_f)]),
     "h4_kernel_launches": (_i, [_vp, C.POINTER(C.c_ulonglong)]),

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/gravidy_gb300.h"
 #include "h4_internal.cuh"
@@ -528,6 +529,32 @@ int h4_upload(h4_handle h, const h4_double4 *r, const h4_double4 *v, const h4_fo
     if (dt) H4_TRY(cudaMemcpyAsync(h->d.dt, dt, N * 8, cudaMemcpyHostToDevice, s), "upload dt");
     H4_TRY(cudaStreamSynchronize(s), "upload");
     if (f) h->forces_ready = true;
+    return H4_OK;
+}
+
+int h4_restore(h4_handle h, const h4_double4 *r, const h4_double4 *v, const h4_forces *f, const double *t,
+               const double *dt, double atime) {
+    if (!h || !r || !v || !f || !t || !dt) return fail(H4_ERR_ARG, "h4_restore: null argument");
+    if (!(atime >= 0.0) || !std::isfinite(atime)) return fail(H4_ERR_ARG, "h4_restore: bad atime");
+    const size_t N = h->d.n;
+    for (size_t i = 0; i < N; i++)
+        if (!(dt[i] > 0.0) || !std::isfinite(t[i]) || !std::isfinite(dt[i]))
+            return fail(H4_ERR_ARG, "h4_restore: bad t/dt at particle " + std::to_string(i));
+    // masses rounded to float as in h4_create
+    std::vector<h4_double4> rr(r, r + N);
+    for (auto &p : rr) p.w = (double)(float)p.w;
+    cudaStream_t s = h->stream;
+    H4_TRY(cudaMemcpyAsync(h->d.r, rr.data(), N * 32, cudaMemcpyHostToDevice, s), "restore r");
+    H4_TRY(cudaMemcpyAsync(h->d.v, v, N * 32, cudaMemcpyHostToDevice, s), "restore v");
+    H4_TRY(cudaMemcpyAsync(h->d.f, f, N * 48, cudaMemcpyHostToDevice, s), "restore f");
+    H4_TRY(cudaMemcpyAsync(h->d.t, t, N * 8, cudaMemcpyHostToDevice, s), "restore t");
+    H4_TRY(cudaMemcpyAsync(h->d.dt, dt, N * 8, cudaMemcpyHostToDevice, s), "restore dt");
+    launch_set_atime(h->d, atime, s);
+    h->launches += 1;
+    int st = check_launch("h4_restore");
+    if (st) return st;
+    H4_TRY(cudaStreamSynchronize(s), "h4_restore");
+    h->forces_ready = true;
     return H4_OK;
 }
 

@@ -37,7 +37,7 @@ __device__ __forceinline__ void predict(double itime, double t, const double *f,
     const double dt = sub(itime, t);
     const double dt2 = mul(dt, dt);
     const double dt3 = mul(dt2, dt);
-    const double dt2c = dvd(dt2, 2.0);
+    const double dt2c = mul(dt2, 0.5);   // == dt2 / 2.0 for every double (scaling by 2^-1)
     const double dt3c = dvd(dt3, 6.0);
     pr.x = add(add(add(mul(dt3c, f[3]), mul(dt2c, f[0])), mul(dt, v.x)), r.x);
     pr.y = add(add(add(mul(dt3c, f[4]), mul(dt2c, f[1])), mul(dt, v.y)), r.y);
@@ -65,11 +65,26 @@ __device__ __forceinline__ void pack_jf(const dbl4 &pr, const dbl4 &pv, float4 &
     c = make_float4((float)pv.x, (float)pv.y, (float)pv.z, 0.f);
 }
 
+// x is a normal power of two (zero mantissa bits).
+__device__ __forceinline__ bool is_pow2(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long e = (b >> 52) & 0x7FFull;
+    return (b & 0x000FFFFFFFFFFFFFull) == 0ull && e != 0ull && e != 0x7FFull && (b >> 63) == 0ull;
+}
+
+// 1/x of a normal power of two x, exactly (exponent arithmetic); requires
+// 1/x to be normal as well.
+__device__ __forceinline__ double recip_pow2(double x) {
+    const long long e = (long long)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FFull);
+    return __longlong_as_double((long long)((unsigned long long)(2046 - e) << 52));
+}
+
 // NbodyUtils::normalize_dt (NbodyUtils.cpp:371-424); dt_min/dt_max are the
 // clamp bounds (D_TIME_MIN/D_TIME_MAX by default).
 __device__ __forceinline__ double normalize_dt(double new_dt, double old_dt, double t, double dt_min,
                                                double dt_max) {
-    const double o8 = dvd(old_dt, 8.0), o4 = dvd(old_dt, 4.0), o2 = dvd(old_dt, 2.0);
+    // x / 2^k == x * 2^-k for every double x: scaling by a power of two
+    const double o8 = mul(old_dt, 0.125), o4 = mul(old_dt, 0.25), o2 = mul(old_dt, 0.5);
     const double o2x = mul(old_dt, 2.0);
     if (new_dt <= o8) {
         new_dt = D_TIME_MIN_REF;
@@ -82,7 +97,7 @@ __device__ __forceinline__ double normalize_dt(double new_dt, double old_dt, dou
     } else if (old_dt < new_dt && new_dt <= o2x) {
         new_dt = old_dt;
     } else if (o2x < new_dt) {
-        const double val = dvd(t, o2x);
+        const double val = is_pow2(o2x) ? mul(t, recip_pow2(o2x)) : dvd(t, o2x);
         new_dt = (ceil(val) == val) ? mul(2.0, old_dt) : old_dt;
     } else {
         new_dt = old_dt;
@@ -105,14 +120,26 @@ __device__ __forceinline__ bool correct(double itime, double eta, double dt_min,
     const double dt3 = mul(dt2, dt1);
     const double dt4 = mul(dt2, dt2);
     const double dt5 = mul(dt4, dt1);
+    // Block timesteps are powers of two, so dt^k is one too (dt >= 2^-23 keeps
+    // every power normal): x / dt^k is then x * (1/dt^k) exactly, and
+    // dt^k / 24 = dt^k * RN(1/24) exactly, since RN(2^m / 3) = 2^m RN(1/3)
+    // (likewise 1/6 and 1/120 = 2^-3 / 15).  Identical results to the
+    // divisions, without the FP64 division sequences; any other dt takes the
+    // divisions.
+    const bool p2 = is_pow2(dt1) && is_pow2(dt5);
+    const double i2 = p2 ? recip_pow2(dt2) : 0.0, i3 = p2 ? recip_pow2(dt3) : 0.0;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         // (-6 (a0 - a1) - dt (4 j0 + 2 j1)) / dt^2
-        a2[c] = dvd(sub(mul(-6.0, sub(o[c], f[c])), mul(dt1, add(mul(4.0, o[3 + c]), mul(2.0, f[3 + c])))), dt2);
+        const double n2 = sub(mul(-6.0, sub(o[c], f[c])), mul(dt1, add(mul(4.0, o[3 + c]), mul(2.0, f[3 + c]))));
         // (12 (a0 - a1) + 6 dt (j0 + j1)) / dt^3
-        a3[c] = dvd(add(mul(12.0, sub(o[c], f[c])), mul(mul(6.0, dt1), add(o[3 + c], f[3 + c]))), dt3);
+        const double n3 = add(mul(12.0, sub(o[c], f[c])), mul(mul(6.0, dt1), add(o[3 + c], f[3 + c])));
+        a2[c] = p2 ? mul(n2, i2) : dvd(n2, dt2);
+        a3[c] = p2 ? mul(n3, i3) : dvd(n3, dt3);
     }
-    const double c24 = dvd(dt4, 24.0), c120 = dvd(dt5, 120.0), c6 = dvd(dt3, 6.0);
+    const double c24 = p2 ? mul(dt4, 0x1.5555555555555p-5) : dvd(dt4, 24.0);
+    const double c120 = p2 ? mul(dt5, 0x1.1111111111111p-7) : dvd(dt5, 120.0);
+    const double c6 = p2 ? mul(dt3, 0x1.5555555555555p-3) : dvd(dt3, 6.0);
     r.x = add(add(p.x, mul(c24, a2[0])), mul(c120, a3[0]));
     r.y = add(add(p.y, mul(c24, a2[1])), mul(c120, a3[1]));
     r.z = add(add(p.z, mul(c24, a2[2])), mul(c120, a3[2]));

@@ -150,7 +150,8 @@ __device__ __forceinline__ void pair_mixed(const IParticle &p, float4 j0, float4
         r2 = self ? 1.0f : r2;
         m = self ? 0.0f : m;
     }
-    const float rinv = rsqrtf(r2);
+    float rinv;   // hardware approximation (MUFU), no denormal range handling
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rinv) : "f"(r2));
     const float r2inv = rinv * rinv;
     const float A = (m * rinv) * r2inv;
     const float rv = fmaf(dx, dvx, fmaf(dy, dvy, dz * dvz));

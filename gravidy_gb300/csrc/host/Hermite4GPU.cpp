@@ -22,6 +22,18 @@ Hermite4GPU::Hermite4GPU(NbodySystem *ns_, Logger *logger_) : ns(ns_), logger(lo
     logger->log_info("GPUs: 1");
 }
 
+Hermite4GPU::Hermite4GPU(NbodySystem *ns_, Logger *logger_, const CheckpointScalars &resume_from)
+    : ns(ns_), logger(logger_), h_(nullptr) {
+    check(h4_create(&h_, ns->n, ns->e2, ns->eta, ns->h_r, ns->h_v, ns->force_mode), "h4_create");
+    check(h4_set_dt_limits(h_, resume_from.dt_min > 0 ? resume_from.dt_min : D_TIME_MIN,
+                           resume_from.dt_max > 0 ? resume_from.dt_max : D_TIME_MAX),
+          "h4_set_dt_limits");
+    check(h4_restore(h_, ns->h_r, ns->h_v, ns->h_f, ns->h_t, ns->h_dt, resume_from.atime), "h4_restore");
+    resumed_ = true;
+    chk_ = resume_from;
+    logger->log_info("resuming at t = " + std::to_string(resume_from.itime));
+}
+
 Hermite4GPU::~Hermite4GPU() { h4_destroy(h_); }
 
 void Hermite4GPU::next_integration_time(double &ATIME) {
@@ -93,20 +105,51 @@ void Hermite4GPU::integration() {
     unsigned int nsteps = 0;
     long long interactions = 0;
     unsigned int output_factor = 1;
-
-    init_acc_jrk();
-    init_dt(ATIME, ETA_S, ITIME);
-    ns->en.ini = get_energy_gpu();
-    ns->en.tmp = ns->en.ini;
-
-    logger->print_info();
-    logger->write_info();
-    logger->print_energy_log(ITIME, (unsigned int)ns->iterations, interactions, nsteps, ns->en.ini);
     unsigned int snap_number = ns->snapshot_number;
-    sync_host();
-    logger->write_snapshot(snap_number, ITIME);
-    snap_number++;
-    if (ns->ops.print_all) logger->print_all(ITIME, snap_number);
+    const std::string chk_path = ns->output_filename + ".chk";
+
+    if (resumed_) {
+        ITIME = chk_.itime;
+        ATIME = chk_.atime;
+        nsteps = (unsigned int)chk_.nsteps;
+        interactions = (long long)chk_.interactions;
+        output_factor = (unsigned int)chk_.output_factor;
+        snap_number = (unsigned int)chk_.snapshot_number;
+        ns->iterations = (long long)chk_.iterations;
+        ns->en.ini = chk_.e_ini;
+        ns->en.tmp = chk_.e_tmp;
+        logger->write_info();   // the energy log is appended to, not restarted
+    } else {
+        init_acc_jrk();
+        init_dt(ATIME, ETA_S, ITIME);
+        ns->en.ini = get_energy_gpu();
+        ns->en.tmp = ns->en.ini;
+        logger->print_info();
+        logger->write_info();
+        logger->print_energy_log(ITIME, (unsigned int)ns->iterations, interactions, nsteps, ns->en.ini);
+        sync_host();
+        logger->write_snapshot(snap_number, ITIME);
+        snap_number++;
+        if (ns->ops.print_all) logger->print_all(ITIME, snap_number);
+    }
+    auto checkpoint = [&]() {
+        CheckpointScalars sc{};
+        sc.e2 = ns->e2;
+        sc.eta = ns->eta;
+        sc.dt_min = D_TIME_MIN;
+        sc.dt_max = D_TIME_MAX;
+        sc.itime = ITIME;
+        sc.atime = ATIME;
+        sc.iterations = (double)ns->iterations;
+        sc.nsteps = nsteps;
+        sc.interactions = (double)interactions;
+        sc.e_ini = ns->en.ini;
+        sc.e_tmp = ns->en.tmp;
+        sc.output_factor = output_factor;
+        sc.snapshot_number = snap_number;
+        sc.t_end = ns->integration_time;
+        write_checkpoint(chk_path, *ns, sc);
+    };
 
     while (ITIME < ns->integration_time) {
         const float t_log_f = ns->interval_time * (float)output_factor;
@@ -138,10 +181,12 @@ void Hermite4GPU::integration() {
             logger->write_snapshot(snap_number, ITIME);
             snap_number++;
             output_factor += 1;
+            checkpoint();
         }
     }
     ns->gtime.integration_end = wall_seconds() - ns->gtime.integration_ini;
     sync_host();
+    checkpoint();
     logger->write_snapshot(snap_number, ITIME);
     logger->add_info("SnapshotNumber:", std::to_string(snap_number));
 }

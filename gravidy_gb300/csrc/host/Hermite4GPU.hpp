@@ -12,6 +12,7 @@
 #include <stdexcept>
 #include <string>
 
+#include "Checkpoint.hpp"
 #include "Logger.hpp"
 #include "NbodySystem.hpp"
 
@@ -26,6 +27,8 @@ class H4Failure : public std::runtime_error {
 class Hermite4GPU {
   public:
     Hermite4GPU(NbodySystem *ns, Logger *logger);
+    // Continue a run from a checkpoint already read into ns (read_checkpoint).
+    Hermite4GPU(NbodySystem *ns, Logger *logger, const CheckpointScalars &resume_from);
     ~Hermite4GPU();
     Hermite4GPU(const Hermite4GPU &) = delete;
     Hermite4GPU &operator=(const Hermite4GPU &) = delete;
@@ -56,6 +59,8 @@ class Hermite4GPU {
     h4_handle handle() const { return h_; }
 
   private:
+    bool resumed_ = false;
+    CheckpointScalars chk_{};
     void check(int status, const char *what);
     h4_handle h_;
 };

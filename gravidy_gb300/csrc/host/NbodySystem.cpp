@@ -16,7 +16,7 @@ NbodySystem::NbodySystem(const OptionsParser &op)
       length_snap(op.length_output_number), force_mode(op.force_mode), host_steps(op.host_steps),
       eta(op.eta), total_mass(0.f), integration_time(op.integration_time), interval_time(op.interval_time),
       snapshot_time(op.snapshot_time), resume(op.resume), max_mass(0.f), input_filename(op.input_filename),
-      output_filename(op.output_filename), h_id(nullptr), h_move(nullptr), h_t(nullptr), h_dt(nullptr),
+      output_filename(op.output_filename), resume_filename(op.resume_filename), h_id(nullptr), h_move(nullptr), h_t(nullptr), h_dt(nullptr),
       h_r(nullptr), h_v(nullptr), h_a2(nullptr), h_a3(nullptr), h_f(nullptr), h_old(nullptr) {
     ops = op.ops;
     // NbodySystem.cpp:50: the product of two floats, kept as a float.

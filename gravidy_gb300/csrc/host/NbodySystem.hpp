@@ -47,6 +47,7 @@ class NbodySystem {
 
     std::string input_filename;
     std::string output_filename;
+    std::string resume_filename;
 
     // Host mirrors (NbodySystem.hpp:112-128).
     unsigned int *h_id;

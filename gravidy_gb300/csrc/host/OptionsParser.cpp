@@ -30,6 +30,7 @@ std::string OptionsParser::usage() const {
       << "Required options:\n"
       << "  -i [ --input ] <filename>      Input data filename\n"
       << "  -t [ --time ] <value> (=1)     Integration time (In N-body units)\n"
+      << "  -r [ --resume ] <file>.chk     Resume a run from its exact checkpoint\n"
       << "Elective options:\n"
       << "  -o [ --output ] <filename>     Output data filename\n"
       << "  -s [ --softening ] <value>     Softening parameter (default 1e-4)\n"
@@ -87,18 +88,24 @@ bool OptionsParser::check_options() {
             else if (m == "mixed") force_mode = H4_FORCE_MIXED;
             else { std::cerr << "gravidy: unknown --mode " << m << std::endl; return false; }
         } else if (is_opt(a, "-r", "--resume")) {
-            std::cerr << "gravidy: --resume is not supported by this build" << std::endl;
-            return false;
+            resume_filename = v;
+            resume = true;
         } else {
             std::cerr << "gravidy: unknown option " << a << "\n" << usage() << std::endl;
             return false;
         }
     }
-    if (!have_input) {
+    if (resume) {
+        if (!file_exists(resume_filename)) {
+            std::cerr << "gravidy: cannot access " << resume_filename << ": No such file or directory" << std::endl;
+            return false;
+        }
+        if (!have_input) input_filename = resume_filename;
+    } else if (!have_input) {
         std::cerr << "gravidy: option requires an argument -- 'input'" << std::endl << usage() << std::endl;
         return false;
     }
-    if (!file_exists(input_filename)) {
+    if (!resume && !file_exists(input_filename)) {
         std::cerr << "gravidy: cannot access " << input_filename << ": No such file or directory" << std::endl;
         return false;
     }

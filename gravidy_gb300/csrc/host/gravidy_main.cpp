@@ -13,13 +13,24 @@ int main(int argc, char *argv[]) {
     OptionsParser op(argc, argv);
     if (!op.check_options()) return 1;
     NbodySystem ns(op);
-    if (!ns.read_input_file()) return 1;
-    ns.alloc_base_attributes(0);
-    ns.copy_input_data();
+    CheckpointScalars chk{};
+    if (op.resume) {
+        // exact continuation: state and loop counters from the checkpoint
+        if (!read_checkpoint(op.resume_filename, ns, chk)) return 1;
+    } else {
+        if (!ns.read_input_file()) return 1;
+        ns.alloc_base_attributes(0);
+        ns.copy_input_data();
+    }
     Logger logger(&ns);
     try {
-        Hermite4GPU h4(&ns, &logger);
-        h4.integration();
+        if (op.resume) {
+            Hermite4GPU h4(&ns, &logger, chk);
+            h4.integration();
+        } else {
+            Hermite4GPU h4(&ns, &logger);
+            h4.integration();
+        }
     } catch (const H4Failure &e) {
         logger.log_error(e.what());
         return 2;

@@ -48,6 +48,7 @@ class NbodySystem:
     ids: np.ndarray | None = None
     snapshot_time: float = 0.0
     iterations: int = 0
+    e2_value: float | None = None   # exact e2 (a resumed run); else from softening
     h_r: np.ndarray = field(init=False)
     h_v: np.ndarray = field(init=False)
 
@@ -71,6 +72,8 @@ class NbodySystem:
 
     @property
     def e2(self) -> float:
+        if self.e2_value is not None:
+            return float(self.e2_value)
         return e2_from_softening(self.softening)
 
     @classmethod
@@ -228,6 +231,34 @@ class Hermite4GPU:
     def upload(self, r=None, v=None, f=None, old=None, t=None, dt=None):
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (r, v, f, old, t, dt)]
         _lib.check(self.L.h4_upload(self.h, *[_lib.ptr(a) for a in arrs]))
+
+    def restore(self, state: dict, atime: float):
+        """Continue from a saved state (r, v, f, t, dt) with next block time
+        atime, without recomputing forces or timesteps."""
+        arrs = [np.ascontiguousarray(state[k], dtype=np.float64) for k in ("r", "v", "f", "t", "dt")]
+        _lib.check(self.L.h4_restore(self.h, *[a.ctypes.data for a in arrs], float(atime)))
+
+    def save_checkpoint(self, path: str, itime: float, atime: float, **scalars):
+        from .checkpoint import write_checkpoint
+        ns = self.ns
+        sc = dict(e2=ns.e2, eta=ns.eta, itime=itime, atime=atime, iterations=ns.iterations,
+                  nsteps=self.nsteps, interactions=self.interactions)
+        sc.update(scalars)
+        write_checkpoint(path, self.download(), sc, ns.ids)
+
+    @classmethod
+    def from_checkpoint(cls, path: str, mode: str = "fp64", **ns_kw):
+        """(integrator, itime, atime, scalars) continuing the saved run."""
+        from .checkpoint import read_checkpoint
+        state, sc, ids = read_checkpoint(path)
+        ns = NbodySystem(state["r"][:, 3], state["r"][:, :3], state["v"][:, :3], ids=ids,
+                         eta=sc["eta"], e2_value=sc["e2"], **ns_kw)
+        g = cls(ns, mode=mode)
+        g.restore(state, sc["atime"])
+        ns.iterations = int(sc["iterations"])
+        g.nsteps = int(sc["nsteps"])
+        g.interactions = int(sc["interactions"])
+        return g, sc["itime"], sc["atime"], sc
 
     def sync_host(self):
         st = self.download()

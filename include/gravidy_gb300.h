@@ -155,6 +155,15 @@ int h4_download(h4_handle h, h4_double4 *r, h4_double4 *v, h4_forces *f,
 int h4_upload(h4_handle h, const h4_double4 *r, const h4_double4 *v,
               const h4_forces *f, const h4_forces *old, const double *t,
               const double *dt);
+/* Resume from a saved state: replaces r, v, f, t, dt (n elements each) and
+ * marks the forces valid, so h4_step/h4_advance continue from *atime
+ * without h4_init_acc_jrk/h4_init_dt.  With the state written by
+ * h4_download the continuation is bit-identical to an uninterrupted run.
+ * (The reference resumes from 4-digit snapshots and recomputes forces and
+ * timesteps, OptionsParser.cpp:122-323, NbodySystem.cpp:106-147.) */
+int h4_restore(h4_handle h, const h4_double4 *r, const h4_double4 *v,
+               const h4_forces *f, const double *t, const double *dt,
+               double atime);
 /* Predicted positions/velocities (Predictor array of the reference,
  * common.hpp:213-218, as two double4 arrays; pr.w = mass). */
 int h4_download_predicted(h4_handle h, h4_double4 *pr, h4_double4 *pv);
