@@ -53,6 +53,9 @@ SIGNATURES = {
     "h4_nact_histogram": (_i, [_vp, _vp]),
     "h4_probe_peaks": (_i, [_pd, _pd]),
     "h4_forces_noalloc": (_i, [_u, _d, _vp, _vp, _u, _vp, _vp, _vp]),
+    "h4_center_of_density": (_i, [_vp, _vp]),
+    "h4_mass_radii": (_i, [_vp, _vp, _f, _pd, _pd, _vp]),
+    "h4_diag_last_error": (C.c_char_p, []),
     "h4_ens_last_error": (C.c_char_p, []),
     "h4_ens_create": (_i, [C.POINTER(_vp), _u, _vp, _vp, _vp, _vp, _vp, _i]),
     "h4_ens_destroy": (_i, [_vp]),

@@ -601,6 +601,16 @@ int h4_forces_for(h4_handle h, const h4_double4 *pr, const h4_double4 *pv, unsig
     return H4_OK;
 }
 
+// Device positions and stream of a handle, for the diagnostics translation
+// unit (not part of the public header).
+int h4_internal_positions(h4_handle h, const void **r, int *n, void **stream) {
+    if (!h) return fail(H4_ERR_ARG, "null handle");
+    *r = h->d.r;
+    *n = h->d.n;
+    *stream = (void *)h->stream;
+    return H4_OK;
+}
+
 int h4_last_timings(h4_handle h, float *force_ms, float *advance_ms) {
     if (!h) return fail(H4_ERR_ARG, "null handle");
     if (force_ms) {

@@ -60,6 +60,8 @@ bool read_checkpoint(const std::string &path, NbodySystem &ns, CheckpointScalars
     }
     ns.e2 = sc.e2;
     ns.eta = (float)sc.eta;
+    ns.total_mass = 0.f;   // as read_input_file sums it: float, in particle order
+    for (uint64_t i = 0; i < n; i++) ns.total_mass += (float)ns.h_r[i].w;
     ns.iterations = (long long)sc.iterations;
     return true;
 }

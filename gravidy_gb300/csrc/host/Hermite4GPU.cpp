@@ -2,6 +2,7 @@
 
 #include <sstream>
 
+#include "NbodyUtils.hpp"
 #include "Timer.hpp"
 
 namespace gb300 {
@@ -132,6 +133,14 @@ void Hermite4GPU::integration() {
         snap_number++;
         if (ns->ops.print_all) logger->print_all(ITIME, snap_number);
     }
+    NbodyUtils nu(ns, h_);
+    if (!resumed_ && nu.nbody_attributes(ns->en.ini)) {
+        std::ostringstream a;
+        a << "r_virial " << nu.r_virial << ", t_cr " << nu.t_cr << ", r_core " << nu.r_core << ", r_hm "
+          << nu.r_hm << ", t_rlx " << nu.t_rlx;
+        logger->log_info(a.str());
+    }
+    if (!resumed_ && ns->ops.print_lagrange && nu.lagrange_radii()) logger->print_lagrange_radii(ITIME, nu.layers_radii);
     auto checkpoint = [&]() {
         CheckpointScalars sc{};
         sc.e2 = ns->e2;
@@ -178,6 +187,7 @@ void Hermite4GPU::integration() {
                                      nsteps - nact, e);
             sync_host();
             if (ns->ops.print_all) logger->print_all(ITIME, snap_number);
+            if (ns->ops.print_lagrange && nu.lagrange_radii()) logger->print_lagrange_radii(ITIME, nu.layers_radii);
             logger->write_snapshot(snap_number, ITIME);
             snap_number++;
             output_factor += 1;

@@ -141,6 +141,19 @@ void Logger::print_energy_log(double ITIME, unsigned int iterations, long long i
     *g << std::setw(12) << std::right << ns->gtime.gflops << std::endl;
 }
 
+void Logger::print_lagrange_radii(double ITIME, const std::vector<double> &radii) {
+    std::ofstream file;
+    std::ostream *g = &std::cout;
+    if (!print_screen) {
+        file.open((ofname + ".radii").c_str(), std::ios::out | std::ios::app);
+        g = &file;
+    }
+    *g << "01 " << std::fixed << ITIME << " ";
+    g->precision(6);
+    for (size_t i = 0; i < radii.size(); i++) *g << std::setw(6) << std::right << radii[i] << " ";
+    *g << std::endl;
+}
+
 void Logger::log(int type, const std::string &msg) {
     static const char *names[] = {" [ERROR] ", " [WARNING] ", " [SUCCESS] ", " [INFO] "};
     static const char *colors[] = {"\033[0;31m", "\033[0;33m", "\033[0;32m", "\033[0;36m"};

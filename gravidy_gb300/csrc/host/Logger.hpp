@@ -9,6 +9,7 @@
 #include <fstream>
 #include <iostream>
 #include <string>
+#include <vector>
 
 #include "NbodySystem.hpp"
 
@@ -31,6 +32,9 @@ class Logger {
     void print_all(double ITIME, unsigned int snapshot_number);
     void print_energy_log(double ITIME, unsigned int iterations, long long interactions, unsigned int nsteps,
                           double new_energy);
+    // Logger::print_lagrange_radii (Logger.cpp:239-268): "01 t r1 .. r6" to
+    // <out>.radii (appended) or the screen.
+    void print_lagrange_radii(double ITIME, const std::vector<double> &radii);
     void log_error(const std::string &msg);
     void log_warning(const std::string &msg);
     void log_success(const std::string &msg);

@@ -38,7 +38,7 @@ std::string OptionsParser::usage() const {
       << "  -p [ --screen ]                Print summary in the screen instead of a file\n"
       << "  -z [ --interval ] <value>      Output time interval (default 0.125)\n"
       << "Extra options:\n"
-      << "  -l [ --lagrange ]              (accepted; Lagrange radii are not computed)\n"
+      << "  -l [ --lagrange ]              Print the Lagrange radii at every output time\n"
       << "  -a [ --all ]                   Print all the information of N-particles\n"
       << "  -g [ --gpu ] <value> (=0)      GPUs to use (one GPU is used)\n"
       << "  --mode fp64|exact|mixed        Force arithmetic (default fp64)\n"

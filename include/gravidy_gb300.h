@@ -249,6 +249,20 @@ int h4_forces_noalloc(unsigned int n, double e2, const h4_double4 *d_pr,
                       void *stream);
 const char *h4_forces_noalloc_error(void);
 
+/* ---- Cluster diagnostics (NbodyUtils, src/include/utils/NbodyUtils.cpp) ----
+ * On the corrected state; nothing here feeds back into the dynamics.
+ * Center of density (get_center_of_density, :163-220): density of every
+ * particle from its 6th-neighbour distance, density-weighted mean position;
+ * needs n >= 8. */
+int h4_center_of_density(h4_handle h, double cod[3]);
+/* Mass radii about `center` (get_core_radius :108-143 with CORE_MASS = 0.1,
+ * get_halfmass_radius :223-260, get_radii + get_layers :285-328 with
+ * LAGRANGE_RADII = {0.01, 0.05, 0.1, 0.2, 0.5, 0.75}); total_mass is
+ * NbodySystem::total_mass (float).  Any output pointer may be NULL. */
+int h4_mass_radii(h4_handle h, const double center[3], float total_mass,
+                  double *core, double *halfmass, double lagrange[6]);
+const char *h4_diag_last_error(void);
+
 /* Device time (ms) of the last force kernel launch and of the last
  * h4_advance call, measured with CUDA events on the handle's stream. */
 int h4_last_timings(h4_handle h, float *force_ms, float *advance_ms);

@@ -493,3 +493,162 @@ unsigned long long orc_state_hash(const orc_system *s)
     }
     return h;
 }
+
+/* ---- diagnostics (NbodyUtils.cpp:59-328) ------------------------------------ */
+
+#define ORC_PI 3.14159265358979323846   /* M_PI of the reference's <cmath> */
+
+typedef struct { int index; double value; } orc_distance;
+
+static int orc_cmp_distance(const void *a, const void *b)
+{
+    const double x = ((const orc_distance *)a)->value, y = ((const orc_distance *)b)->value;
+    return (x < y) ? -1 : (x > y) ? 1 : 0;
+}
+
+float orc_total_mass(const orc_system *s)
+{
+    float m = 0.0f;   /* NbodySystem.cpp:182: float += float (the parsed mass) */
+    for (unsigned int i = 0; i < s->n; i++) m += (float)s->r[i].w;
+    return m;
+}
+
+/* NbodyUtils::get_center_of_density, NbodyUtils.cpp:163-220 (J = 6,
+ * common.hpp:94): density from the 6th neighbour distance, float radius and
+ * density, float sum of the densities. */
+void orc_center_of_density(const orc_system *s, double cod[3])
+{
+    const unsigned int n = s->n;
+    const int J = 6;
+    double *p = (double *)calloc(n ? n : 1, sizeof(double));
+    long nn = (long)n;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long i = 0; i < nn; i++) {
+        /* the J+1 smallest entries of d (self = 0 included), kept sorted */
+        double best[7];
+        for (int k = 0; k < 7; k++) best[k] = INFINITY;
+        best[0] = 0.0;   /* d[i] keeps the zero-valued default entry */
+        int cnt = 1;
+        for (unsigned int j = 0; j < n; j++) {
+            if ((long)j == i) continue;
+            double rx = (s->r[j].x - s->r[i].x);
+            double ry = (s->r[j].y - s->r[i].y);
+            double rz = (s->r[j].z - s->r[i].z);
+            double v = sqrt(rx * rx + ry * ry + rz * rz);
+            if (cnt < 7 || v < best[6]) {
+                int k = cnt < 7 ? cnt++ : 6;
+                while (k > 0 && best[k - 1] > v) { best[k] = best[k - 1]; k--; }
+                best[k] = v;
+            }
+        }
+        float radius = (float)best[J];
+        float aa = (J - 1) * s->r[i].w;
+        float bb = (4.0 * ORC_PI * radius * radius * radius) / 3.0;
+        p[i] = aa / bb;
+    }
+    double cx = 0.0, cy = 0.0, cz = 0.0;
+    float dsum = 0.0f;
+    for (unsigned int i = 0; i < n; i++) {
+        dsum += p[i];
+        cx += s->r[i].x * p[i];
+        cy += s->r[i].y * p[i];
+        cz += s->r[i].z * p[i];
+    }
+    cod[0] = cx / dsum;
+    cod[1] = cy / dsum;
+    cod[2] = cz / dsum;
+    free(p);
+}
+
+/* get_core_radius (:108-143), get_halfmass_radius (:223-260) and
+ * get_radii + get_layers (:285-328) about `center`.  The reference's layer
+ * loop runs past its 6 layers; this one stops there. */
+void orc_mass_radii(const orc_system *s, const double center[3], float total_mass, double *core,
+                    double *halfmass, double lagrange[6])
+{
+    static const float LAGRANGE[6] = {0.01f, 0.05f, 0.1f, 0.2f, 0.5f, 0.75f};
+    const float CORE_MASS = 0.1f;
+    const unsigned int n = s->n;
+    orc_distance *d = (orc_distance *)malloc(sizeof(orc_distance) * (n ? n : 1));
+    for (unsigned int i = 0; i < n; i++) {
+        double rx = s->r[i].x - center[0];
+        double ry = s->r[i].y - center[1];
+        double rz = s->r[i].z - center[2];
+        d[i].index = (int)i;
+        d[i].value = sqrt(rx * rx + ry * ry + rz * rz);
+    }
+    qsort(d, n, sizeof(orc_distance), orc_cmp_distance);
+    /* core radius */
+    double core_mass = 0.0, radius = 0.0;
+    for (unsigned int i = 0; i < n; i++) {
+        if (core_mass > total_mass * CORE_MASS) {
+            radius = d[i - 1].value;
+            break;
+        }
+        core_mass += s->r[d[i].index].w;
+    }
+    *core = radius;
+    /* half-mass radius */
+    float half_mass = 0.0f;
+    unsigned int jh = 0;
+    for (unsigned int i = 0; i < n; i++) {
+        if (half_mass >= total_mass / 2.0) {
+            jh = i;
+            break;
+        }
+        half_mass += s->r[d[i].index].w;
+    }
+    *halfmass = jh > 0 ? d[jh - 1].value : 0.0;
+    /* Lagrange radii */
+    float tmp_mass = 0.0f;
+    unsigned int layer = 0;
+    for (int k = 0; k < 6; k++) lagrange[k] = 0.0;
+    for (unsigned int i = 0; i < n && layer < 6; i++) {
+        if (tmp_mass >= total_mass) break;
+        if (tmp_mass > LAGRANGE[layer]) {
+            lagrange[layer] = d[i].value;
+            layer += 1;
+        }
+        tmp_mass += s->r[d[i].index].w;
+    }
+    free(d);
+}
+
+/* NbodyUtils::nbody_attributes, NbodyUtils.cpp:59-78, with
+ * get_virial_radius (:81-86), get_crossing_time (:88-97),
+ * get_close_encounter_radius/_timestep (:99-110) and
+ * get_half_mass_relaxation_time (:145-160). */
+void orc_nbody_attributes(const orc_system *s, double e_ini, float total_mass, double cod_state[3],
+                          orc_attributes *out)
+{
+    const int G = 1;
+    const unsigned int n = s->n;
+    double lag[6], core, core2, half;
+    float r_virial = (-G * total_mass * total_mass) / (4 * e_ini);
+    float M = total_mass;
+    float Rv3 = (double)r_virial * (double)r_virial * (double)r_virial;
+    float Ut = sqrt(Rv3 / (G * M));
+    float t_cr = 2 * sqrt(2) * Ut;
+    double r_cl = (4.0 * (double)r_virial) / n;
+    float r_cl3 = r_cl * r_cl * r_cl;
+    double dt_cl = 0.04 * sqrt(r_cl3 * n);
+    /* core radius about the NbodyUtils::cod held on entry */
+    orc_mass_radii(s, cod_state, total_mass, &core, &half, lag);
+    /* relaxation time: center of density first, then the half-mass radius */
+    orc_center_of_density(s, cod_state);
+    orc_mass_radii(s, cod_state, total_mass, &core2, &half, lag);
+    float r_h = half;
+    float a = sqrt((n * r_h * r_h * r_h) / (G * (total_mass / (n))));
+    float b = 1 / log(0.11 * n);
+    float t_rh = 0.138 * a * b;
+    out->r_virial = r_virial;
+    out->t_cr = t_cr;
+    out->r_cl = r_cl;
+    out->dt_cl = dt_cl;
+    out->r_core = core;
+    out->t_rlx = t_rh;
+    out->r_hm = r_h;
+    out->cod[0] = cod_state[0];
+    out->cod[1] = cod_state[1];
+    out->cod[2] = cod_state[2];
+}

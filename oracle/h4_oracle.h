@@ -92,6 +92,25 @@ typedef struct {
 int orc_integrate(orc_system *s, float t_end, float interval, orc_run_stats *st,
                   double *rows, int max_rows);
 
+/* Diagnostics of NbodyUtils (src/include/utils/NbodyUtils.cpp:59-328), with
+ * the reference's float/double types.  total_mass is NbodySystem::total_mass
+ * (a float summed in input order, NbodySystem.cpp:182).  Need n >= 8 (the
+ * reference reads the 6th neighbour, and crashes below that). */
+float orc_total_mass(const orc_system *s);
+void orc_center_of_density(const orc_system *s, double cod[3]);
+/* Core radius (mass fraction CORE_MASS = 0.1, strict), half-mass radius and
+ * Lagrange radii (LAGRANGE_RADII = 0.01 .. 0.75) about `center`. */
+void orc_mass_radii(const orc_system *s, const double center[3], float total_mass, double *core,
+                    double *halfmass, double lagrange[6]);
+typedef struct {
+    double r_virial, t_cr, r_cl, dt_cl, r_core, t_rlx, r_hm;
+    double cod[3];
+} orc_attributes;
+/* NbodyUtils::nbody_attributes: cod_state is NbodyUtils::cod, in and out
+ * (the core radius uses its value on entry, then it is recomputed). */
+void orc_nbody_attributes(const orc_system *s, double e_ini, float total_mass, double cod_state[3],
+                          orc_attributes *out);
+
 /* FNV-1a 64 over raw bytes, and over the state record
  * (r.x r.y r.z r.w v.x v.y v.z a[3] a1[3] t dt per particle, 15 doubles),
  * the layout written by oracle/ref_harness.cpp. */

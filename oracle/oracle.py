@@ -80,6 +80,10 @@ def lib():
             "orc_block_step": (u, [P, C.POINTER(d), C.POINTER(d)]),
             "orc_integrate": (C.c_int, [P, f, f, C.POINTER(RunStats), vp, C.c_int]),
             "orc_fnv1a": (C.c_ulonglong, [vp, C.c_size_t, C.c_ulonglong]),
+            "orc_total_mass": (f, [P]),
+            "orc_center_of_density": (None, [P, vp]),
+            "orc_mass_radii": (None, [P, vp, f, C.POINTER(d), C.POINTER(d), vp]),
+            "orc_nbody_attributes": (None, [P, d, f, vp, vp]),
             "orc_state_hash": (C.c_ulonglong, [P]),
             "orc_state_record": (None, [P, vp]),
         }
@@ -207,6 +211,29 @@ class Oracle:
         k = lib().orc_integrate(self._s, C.c_float(t_end), C.c_float(interval), C.byref(st),
                                 rows.ctypes.data, max_rows)
         return st, rows[:k].copy()
+
+    def total_mass(self) -> float:
+        return lib().orc_total_mass(self._s)
+
+    def center_of_density(self) -> np.ndarray:
+        out = np.zeros(3)
+        lib().orc_center_of_density(self._s, out.ctypes.data)
+        return out
+
+    def mass_radii(self, center, total_mass: float):
+        c = np.ascontiguousarray(center, dtype=np.float64)
+        core, half = C.c_double(), C.c_double()
+        lag = np.zeros(6)
+        lib().orc_mass_radii(self._s, c.ctypes.data, C.c_float(total_mass), C.byref(core), C.byref(half),
+                             lag.ctypes.data)
+        return core.value, half.value, lag
+
+    def nbody_attributes(self, e_ini: float, total_mass: float, cod_state: np.ndarray) -> np.ndarray:
+        """[r_virial, t_cr, r_cl, dt_cl, r_core, t_rlx, r_hm, cod.x, cod.y, cod.z];
+        cod_state is updated in place (NbodyUtils::cod)."""
+        out = np.zeros(10)
+        lib().orc_nbody_attributes(self._s, e_ini, C.c_float(total_mass), cod_state.ctypes.data, out.ctypes.data)
+        return out
 
     def state_hash(self) -> int:
         return lib().orc_state_hash(self._s)

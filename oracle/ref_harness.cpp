@@ -20,6 +20,10 @@
  *                for the first nfull steps and for every logged step
  *   energy.txt : "itime energy" at t=0 and at every log time (hex floats)
  *   state_<k>.bin for each requested step k (and 'final' at the end)
+ *   attributes.txt : for N >= 8, NbodyUtils::nbody_attributes and
+ *                lagrange_radii (NbodyUtils.cpp:59-78, 246-328) after the
+ *                initial energy and again at the end, in the reference's
+ *                call order (hex floats)
  */
 #include "cpu/Hermite4CPU.hpp"
 #include <cstdio>
@@ -53,6 +57,18 @@ static uint64_t state_hash(NbodySystem *ns)
         h = fnv1a(rec, sizeof(rec), h);
     }
     return h;
+}
+
+static void write_attributes(FILE *fa, const char *tag, NbodySystem *ns, NbodyUtils *nu)
+{
+    nu->nbody_attributes();
+    std::fprintf(fa, "%s_attr %a %a %a %a %a %a %a %a %a %a\n", tag, (double)ns->r_virial, (double)ns->t_cr,
+                 ns->r_cl, ns->dt_cl, ns->r_core, (double)ns->t_rlx, (double)ns->r_hm, nu->cod.x, nu->cod.y,
+                 nu->cod.z);
+    nu->lagrange_radii();
+    std::fprintf(fa, "%s_lagr", tag);
+    for (size_t k = 0; k < nu->layers_radii.size(); k++) std::fprintf(fa, " %a", nu->layers_radii[k]);
+    std::fprintf(fa, " %a %a %a\n", nu->cod.x, nu->cod.y, nu->cod.z);
 }
 
 static void write_state(NbodySystem *ns, const std::string &path)
@@ -122,6 +138,14 @@ int main(int argc, char *argv[])
     }
     ns.en.ini = nu.get_energy(0);
     ns.en.tmp = ns.en.ini;
+    FILE *fa = 0;
+    if (ns.n >= 8) {
+        std::string apath = outdir + "/attributes.txt";
+        fa = std::fopen(apath.c_str(), "w");
+        if (!fa) { std::perror("attributes"); return 2; }
+        std::fprintf(fa, "total_mass %a\n", (double)ns.total_mass);
+        write_attributes(fa, "t0", &ns, &nu);
+    }
 
     std::string spath = outdir + "/steps.txt";
     std::string epath = outdir + "/energy.txt";
@@ -162,6 +186,10 @@ int main(int argc, char *argv[])
         step++;
     }
     write_state(&ns, outdir + "/state_final.bin");
+    if (fa) {
+        write_attributes(fa, "end", &ns, &nu);
+        std::fclose(fa);
+    }
     std::fprintf(fs, "# steps %ld nsteps %u interactions %lld\n", step, nsteps, interactions);
     std::fclose(fs);
     std::fclose(fe);

@@ -58,3 +58,17 @@ def test_cli_fp64_energy_error_matches_reference(tmp_path):
     assert [r[0] for r in rows] == [r[0] for r in ref]
     cum, cum_ref = rows[-1][5], float(ref[-1][5])
     assert abs(cum - cum_ref) <= 1e-2 * cum_ref
+
+
+def test_cli_lagrange_radii_file(tmp_path):
+    """-l writes the Lagrange radii at t = 0 and every output time in the
+    reference's format; the t = 0 row equals the reference's values."""
+    name = "c1_plummer_n1024"
+    _, out = _run(tmp_path, name, "exact", ("-l",))
+    rows = [l.split() for l in open(out + ".out.radii")]
+    assert len(rows) == 1 + 8 and all(r[0] == "01" and len(r) == 8 for r in rows)
+    want = None
+    for line in open(os.path.join(case_dir(name), "attributes.txt")):
+        if line.startswith("t0_lagr"):
+            want = [float.fromhex(t) for t in line.split()[1:7]]
+    assert [float(x) for x in rows[0][2:8]] == pytest.approx(want, rel=1e-5, abs=1e-6)

@@ -79,3 +79,40 @@ def test_energy_log_columns_match_reference_program(name):
         mine.append(tuple(text[1:7]))
     ref = load_cli_log(name)
     assert mine == ref
+
+
+def _attributes(name):
+    rows = {}
+    with open(case_dir(name) + "/attributes.txt") as fh:
+        for line in fh:
+            tok = line.split()
+            rows[tok[0]] = [float.fromhex(t) for t in tok[1:]]
+    return rows
+
+
+@pytest.mark.parametrize("name", ["c1_plummer_n1024", "salpeter_n100", "ragged_n33"])
+def test_diagnostics_bit_exact(name):
+    """nbody_attributes and lagrange_radii (NbodyUtils.cpp:59-328) at t = 0
+    and at the end, in the reference's call order (the core radius uses the
+    center of density left by the previous call)."""
+    c = CASES[name]
+    want = _attributes(name)
+    c_, data, o = _make(name)
+    tm = o.total_mass()
+    assert tm == want["total_mass"][0]
+    cod_state = np.zeros(3)
+    o.init_acc_jrk()
+    atime = o.init_dt(0.0, float(orc.ETA_S))
+    e0, _, _ = o.energy()
+    for tag in ("t0", "end"):
+        attr = o.nbody_attributes(e0, tm, cod_state)
+        assert list(attr) == want[f"{tag}_attr"], tag
+        cod = o.center_of_density()
+        core, half, lag = o.mass_radii(cod, tm)
+        assert list(lag) + list(cod) == want[f"{tag}_lagr"], tag
+        cod_state[:] = cod
+        if tag == "t0":
+            itime = 0.0
+            t_end = np.float32(c["t_end"])
+            while itime < t_end:
+                _, itime, atime = o.block_step(itime, atime)
