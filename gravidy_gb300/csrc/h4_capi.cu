@@ -70,7 +70,7 @@ namespace {
 
 void free_device(h4_system_s *h) {
     H4Dev &d = h->d;
-    void *ptrs[] = {d.r, d.v, d.f, d.old, d.a2, d.a3, d.t, d.dt, d.pr, d.pv, d.jf0, d.jf1, d.jf2,
+    void *ptrs[] = {d.r, d.v, d.f, d.old, d.a2, d.a3, d.t, d.dt, d.pr, d.pv, d.jf0, d.jf1, d.jf2, d.jd,
                     d.move, d.blk_cnt, d.part, d.epot_i, d.energy_out, d.ctrl};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -224,7 +224,7 @@ int h4_create(h4_handle *out, unsigned int n, double e2, float eta, const h4_dou
         {(void **)&d.t, N * sizeof(double)},     {(void **)&d.dt, N * sizeof(double)},
         {(void **)&d.pr, NP * sizeof(dbl4)},     {(void **)&d.pv, NP * sizeof(dbl4)},
         {(void **)&d.jf0, NP * sizeof(float4)},  {(void **)&d.jf1, NP * sizeof(float4)},
-        {(void **)&d.jf2, NP * sizeof(float4)},
+        {(void **)&d.jf2, NP * sizeof(float4)},  {(void **)&d.jd, 5 * NP * sizeof(float4)},
         {(void **)&d.move, N * sizeof(unsigned)}, {(void **)&d.blk_cnt, (size_t)nflag * sizeof(unsigned)},
         {(void **)&d.part, d.part_cap * sizeof(double)}, {(void **)&d.epot_i, N * sizeof(double)},
         {(void **)&d.energy_out, 2 * sizeof(double)}, {(void **)&d.ctrl, sizeof(H4Ctrl)},

@@ -217,6 +217,213 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled(H4Dev d, unsigned t
     }
 }
 
+// ---- packed f32x2 variant of the tiled shape (e2 > 0) ----------------------------
+// Two active particles share one 64-bit register pair and every FP32
+// operation of the pair formula is one packed f32x2 instruction (sm_100+),
+// which halves the issue slots the tiled kernel is bound by.  The j data come
+// pre-duplicated from d.jd, so one 128-bit shared load gives two packed
+// operands.  Same arithmetic per lane as pair_mixed (and hence the same
+// results up to the order of the FP32 partial sums, which is identical here).
+
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 pk2(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float lo2(f2 v) {
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return a;
+}
+__device__ __forceinline__ float hi2(f2 v) {
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return b;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ f2 rsqrt2(f2 v) {
+    float a, b, ra, rb;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(ra) : "f"(a));
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rb) : "f"(b));
+    return pk2(ra, rb);
+}
+// 128-bit shared load as two packed operands
+__device__ __forceinline__ void lds2(const float4 *p, f2 &a, f2 &b) {
+    asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(smem_addr(p)));
+}
+
+struct IPair {   // two active particles, packed
+    f2 xh, yh, zh, xl, yl, zl, vx, vy, vz;
+};
+
+__device__ __forceinline__ void kahan2(f2 &s, f2 &c, f2 x) {
+    const f2 y = sub2(x, c);
+    const f2 t = add2(s, y);
+    c = sub2(sub2(t, s), y);
+    s = t;
+}
+
+__device__ __forceinline__ void pair_x2(const IPair &p, f2 jxh, f2 jyh, f2 jzh, f2 jm, f2 jxl, f2 jyl, f2 jzl,
+                                        f2 jvx, f2 jvy, f2 jvz, f2 e2, f2 m3, f2 sum[6]) {
+    const f2 dx = add2(sub2(jxh, p.xh), sub2(jxl, p.xl));
+    const f2 dy = add2(sub2(jyh, p.yh), sub2(jyl, p.yl));
+    const f2 dz = add2(sub2(jzh, p.zh), sub2(jzl, p.zl));
+    const f2 dvx = sub2(jvx, p.vx), dvy = sub2(jvy, p.vy), dvz = sub2(jvz, p.vz);
+    const f2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+    const f2 rinv = rsqrt2(r2);
+    const f2 r2inv = mul2(rinv, rinv);
+    const f2 A = mul2(mul2(jm, rinv), r2inv);
+    const f2 rv = fma2(dx, dvx, fma2(dy, dvy, mul2(dz, dvz)));
+    const f2 eta = mul2(rv, mul2(m3, r2inv));
+    sum[0] = fma2(A, dx, sum[0]);
+    sum[1] = fma2(A, dy, sum[1]);
+    sum[2] = fma2(A, dz, sum[2]);
+    sum[3] = fma2(A, fma2(eta, dx, dvx), sum[3]);
+    sum[4] = fma2(A, fma2(eta, dy, dvy), sum[4]);
+    sum[5] = fma2(A, fma2(eta, dz, dvz), sum[5]);
+}
+
+constexpr int IPT2 = 4;            // active particles per thread (2 packed pairs)
+constexpr int NPK = IPT2 / 2;
+
+__global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled_x2(H4Dev d, unsigned threshold) {
+    __shared__ __align__(128) float4 sj[2][5][JT];
+    __shared__ __align__(8) uint64_t full[2];
+    __shared__ unsigned s_item;
+    const unsigned nact = d.ctrl->nact;
+    if (nact == 0 || nact < threshold) return;
+    const MixedSplit sp = tiled_split(d, nact, gridDim.x);
+    const int tid = threadIdx.x;
+    if (blockIdx.x == 0 && tid == 0) {
+        d.ctrl->force_split = sp.split;
+        d.ctrl->work_total = sp.total;
+    }
+    if (tid == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const float e2f = (float)d.e2;
+    const f2 e2 = pk2(e2f, e2f), m3 = pk2(-3.0f, -3.0f);
+    const size_t np = (size_t)d.n_pad;
+    unsigned gt = 0;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(&d.ctrl->work_next, 1u);
+        __syncthreads();
+        const unsigned item = s_item;
+        __syncthreads();
+        if (item >= sp.total) break;
+        const unsigned s = item / sp.n_groups;
+        const unsigned g = item - s * sp.n_groups;
+        const int j_begin = (int)s * sp.chunk;
+        const int j_end = min(d.n_pad, j_begin + sp.chunk);
+        const int ntiles = (j_end - j_begin) / JT;
+
+        IPair ip[NPK];
+        f2 S[NPK][6], Cc[NPK][6];
+#pragma unroll
+        for (int q = 0; q < NPK; q++) {
+            const unsigned k0 = g * TI + tid + (2 * q) * MT, k1 = k0 + MT;
+            const IParticle a = load_i(d, d.move[k0 < nact ? k0 : nact - 1]);
+            const IParticle b = load_i(d, d.move[k1 < nact ? k1 : nact - 1]);
+            ip[q].xh = pk2(a.xh, b.xh); ip[q].yh = pk2(a.yh, b.yh); ip[q].zh = pk2(a.zh, b.zh);
+            ip[q].xl = pk2(a.xl, b.xl); ip[q].yl = pk2(a.yl, b.yl); ip[q].zl = pk2(a.zl, b.zl);
+            ip[q].vx = pk2(a.vx, b.vx); ip[q].vy = pk2(a.vy, b.vy); ip[q].vz = pk2(a.vz, b.vz);
+#pragma unroll
+            for (int c = 0; c < 6; c++) { S[q][c] = 0ull; Cc[q][c] = 0ull; }
+        }
+        if (tid == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            for (int t = 0; t < 2 && t < ntiles; t++) {
+                const unsigned b = (gt + t) & 1u;
+                const size_t j0 = (size_t)j_begin + (size_t)t * JT;
+                mbar_arrive_expect_tx(&full[b], 5 * JT * sizeof(float4));
+#pragma unroll
+                for (int pl = 0; pl < 5; pl++)
+                    tma_load_1d(&sj[b][pl][0], d.jd + pl * np + j0, JT * sizeof(float4), &full[b]);
+            }
+        }
+        for (int t = 0; t < ntiles; t++, gt++) {
+            const unsigned b = gt & 1u, parity = (gt >> 1) & 1u;
+            unsigned spins = 0;
+            bool ok = true;
+            while (!mbar_try_wait(&full[b], parity)) {
+                if (++spins > WAIT_LIMIT) { ok = false; break; }
+            }
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_TIMEOUT);
+                return;
+            }
+#pragma unroll 1
+            for (int sb = 0; sb < JT; sb += SUB) {
+                f2 part[NPK][6];
+#pragma unroll
+                for (int q = 0; q < NPK; q++)
+#pragma unroll
+                    for (int c = 0; c < 6; c++) part[q][c] = 0ull;
+#pragma unroll 4
+                for (int jj = sb; jj < sb + SUB; jj++) {
+                    f2 jxh, jyh, jzh, jm, jxl, jyl, jzl, jvx, jvy, jvz;
+                    lds2(&sj[b][0][jj], jxh, jyh);
+                    lds2(&sj[b][1][jj], jzh, jm);
+                    lds2(&sj[b][2][jj], jxl, jyl);
+                    lds2(&sj[b][3][jj], jzl, jvx);
+                    lds2(&sj[b][4][jj], jvy, jvz);
+#pragma unroll
+                    for (int q = 0; q < NPK; q++)
+                        pair_x2(ip[q], jxh, jyh, jzh, jm, jxl, jyl, jzl, jvx, jvy, jvz, e2, m3, part[q]);
+                }
+#pragma unroll
+                for (int q = 0; q < NPK; q++)
+#pragma unroll
+                    for (int c = 0; c < 6; c++) kahan2(S[q][c], Cc[q][c], part[q][c]);
+            }
+            __syncthreads();   // every thread is done with buffer b
+            if (tid == 0 && t + 2 < ntiles) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const size_t j0 = (size_t)j_begin + (size_t)(t + 2) * JT;
+                mbar_arrive_expect_tx(&full[b], 5 * JT * sizeof(float4));
+#pragma unroll
+                for (int pl = 0; pl < 5; pl++)
+                    tma_load_1d(&sj[b][pl][0], d.jd + pl * np + j0, JT * sizeof(float4), &full[b]);
+            }
+        }
+        double *p = d.part + (size_t)s * 6 * nact;
+#pragma unroll
+        for (int q = 0; q < NPK; q++) {
+            const unsigned k0 = g * TI + tid + (2 * q) * MT, k1 = k0 + MT;
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                if (k0 < nact) p[(size_t)c * nact + k0] = (double)lo2(S[q][c]) - (double)lo2(Cc[q][c]);
+                if (k1 < nact) p[(size_t)c * nact + k1] = (double)hi2(S[q][c]) - (double)hi2(Cc[q][c]);
+            }
+        }
+    }
+}
+
 // ---- warp items: small active sets --------------------------------------------
 __device__ __forceinline__ MixedSplit warp_split(const H4Dev &d, unsigned nact, unsigned total_warps) {
     MixedSplit s;
@@ -287,6 +494,8 @@ int launch_force_mixed(const H4Dev &d, int num_sms, unsigned threshold, long lon
     if (want_tiled) {
         if (mask)
             k_force_mixed_tiled<true><<<num_sms * 3, MT, 0, s>>>(d, threshold);
+        else if (d.jd)
+            k_force_mixed_tiled_x2<<<num_sms * 3, MT, 0, s>>>(d, threshold);
         else
             k_force_mixed_tiled<false><<<num_sms * 3, MT, 0, s>>>(d, threshold);
         launched++;

@@ -60,6 +60,9 @@ struct H4Dev {
     dbl4 *pr, *pv;       // [n_pad] predicted position (w = mass), velocity
     float4 *jf0, *jf1, *jf2; // [n_pad] predicted j data for the mixed kernels:
                              // (x_hi, y_hi, z_hi, m), (x_lo, y_lo, z_lo, 0), (vx, vy, vz, 0)
+    float4 *jd;              // [5][n_pad] the same j data with every value twice, for
+                             // packed f32x2 arithmetic: (xh,xh,yh,yh), (zh,zh,m,m),
+                             // (xl,xl,yl,yl), (zl,zl,vx,vx), (vy,vy,vz,vz)
     unsigned int *move;     // [n] active list
     unsigned int *blk_cnt;  // [n_blocks_flag] active count per chunk
     double *part;           // partial forces, [S][6][nact] for the current step

@@ -76,6 +76,14 @@ __device__ __forceinline__ void write_jf(const H4Dev &d, int i, const dbl4 &pr, 
     d.jf0[i] = a;
     d.jf1[i] = b;
     d.jf2[i] = c;
+    if (d.jd) {
+        const size_t np = (size_t)d.n_pad;
+        d.jd[i] = make_float4(a.x, a.x, a.y, a.y);
+        d.jd[np + i] = make_float4(a.z, a.z, a.w, a.w);
+        d.jd[2 * np + i] = make_float4(b.x, b.x, b.y, b.y);
+        d.jd[3 * np + i] = make_float4(b.z, b.z, c.x, c.x);
+        d.jd[4 * np + i] = make_float4(c.y, c.y, c.z, c.z);
+    }
 }
 
 // ---- active set (Hermite4::find_particles_to_move) --------------------------
@@ -171,11 +179,7 @@ __global__ void k_pad_predicted(H4Dev d) {
     if (i >= d.n_pad) return;
     d.pr[i] = make_dbl4(1.0e15, 1.0e15, 1.0e15, 0.0);
     d.pv[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);
-    if (d.jf0) {
-        d.jf0[i] = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 0.f);
-        d.jf1[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        d.jf2[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
+    if (d.jf0) write_jf(d, i, d.pr[i], d.pv[i]);
 }
 
 __global__ void k_identity_move(H4Dev d) {
