@@ -5,17 +5,22 @@
 // The per-system arithmetic is the single-system path's (exact-order
 // predictor/corrector/timestep of h4_exact.cuh, force items of h4_pair.cuh);
 // what changes is the schedule.  One iteration of k_ensemble does one block
-// step of every unfinished system, in three phases separated by grid-wide
+// step of every unfinished system, in four phases separated by grid-wide
 // barriers:
-//   P0  per system (one block): block time = next time, ordered active set,
-//       predictor of all its particles, force work layout from the tuning
-//       table (particles per warp item, j-chunk length) for its (N, N_act);
-//   P1  all blocks: warp items of every system's force sum, taken from one
-//       global work queue (the systems' item counts are prefix-summed in
-//       shared memory; an item finds its system by binary search);
-//   P2  per system (the same block as P0): fixed-order reduction of the
-//       partial forces, save of the old forces, corrector, new timesteps, and
-//       the system's next block time.
+//   A  per system (one block): next block time (min t + dt), the reference's
+//      loop condition, ordered active set, force work layout for its
+//      (N, N_act): warp items from the tuning table, or block-tiled items
+//      (mixed form, N_act >= 512);
+//   B  all threads: predictor of every particle of the stepping systems;
+//   C  all blocks: the force sums -- block-tiled items (shared-memory j tiles,
+//      packed f32x2) then warp items, each from one global work queue (the
+//      systems' item counts are prefix-summed in shared memory, an item finds
+//      its system by binary search);
+//   D  all threads: fixed-order reduction of the partial forces, save of the
+//      old forces, corrector and new timestep of every active particle.
+// The O(N) and O(N_act) phases are spread over the whole GPU: FP64
+// prediction and correction of a large system on one SM would otherwise set
+// the pace of every iteration.
 // The kernel is launched cooperatively (all blocks resident), and its grid
 // barriers are bounded waits on the global timer: a barrier that waits longer
 // than BARRIER_TIMEOUT_NS records H4_ERRBIT_TIMEOUT and every block leaves.
@@ -42,7 +47,11 @@ constexpr int NB_N = H4_ENS_TUNE_NB_N;
 constexpr int NB_A = H4_ENS_TUNE_NB_A;
 constexpr unsigned long long BARRIER_TIMEOUT_NS = 60ull * 1000000000ull;
 constexpr int ITERS_PER_LAUNCH = 16;
-constexpr unsigned MAX_SYSTEMS = 8192;
+constexpr unsigned MAX_SYSTEMS = 4096;
+constexpr unsigned BLOCK_MIN_NACT = 512;   // mixed form: block-tiled items from this N_act
+constexpr int BTI = 2 * THREADS;           // active particles per block item (one packed pair per thread)
+constexpr int BJT = 256;                   // j per shared-memory tile of a block item
+constexpr int BCHUNK = 2048;               // j per block item
 
 struct System {
     int off, n;                  // particle offset and count
@@ -51,6 +60,7 @@ struct System {
     double itime, atime;         // last block time, next block time
     unsigned nact;
     unsigned ig, chunk, split, n_groups, items;
+    unsigned bitems;             // block-tiled force items (mixed form, large N_act)
     unsigned done, err;
     size_t part_off, part_cap;   // partial-force area (doubles)
     unsigned long long steps, psteps, inter;
@@ -62,9 +72,11 @@ struct Dev {
     dbl4 *r, *v, *pr, *pv;
     double *f, *old, *a2, *a3, *t, *dt;
     float4 *jf0, *jf1, *jf2;
+    float4 *jd;                  // [5][total] duplicated j data of the block-tiled items
     unsigned *move;
     double *part;
-    unsigned *queue;             // force work-queue head
+    unsigned *queue;             // force work-queue head (warp items)
+    unsigned *queue_b;           // force work-queue head (block items)
     unsigned *bar_count, *bar_gen;
     unsigned *err;               // global error bits
     unsigned *tune_ig, *tune_chunk;   // [NB_N * NB_A]
@@ -157,23 +169,48 @@ __device__ unsigned block_scan_u(unsigned x, unsigned *red, unsigned *total) {
     return before + incl - x;
 }
 
-// ---- P0: active set, predictor, work layout of one system -------------------
+// ---- phase A (one block per system): next block time, ordered active set,
+// bookkeeping and force work layout -------------------------------------------
 template <int MODE>
-__device__ void phase0(const Dev &d, int c, bool init, unsigned *red) {
+__device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *redd) {
     System &S = d.sys[c];
-    if (S.done) {
-        if (threadIdx.x == 0) S.items = 0;
-        return;
-    }
     const int off = S.off, n = S.n;
-    const double itime = init ? 0.0 : S.atime;
-    unsigned nact = 0;
     const unsigned forced = *d.forced_nact;
+    unsigned nact = 0;
+    double itime = 0.0;
     if (init || forced) {
+        if (!init && S.done) {
+            if (threadIdx.x == 0) { S.items = 0; S.bitems = 0; S.nact = 0; }
+            return;
+        }
         const int na = init ? n : (int)min((unsigned)n, forced);
         for (int i = threadIdx.x; i < na; i += THREADS) d.move[off + i] = (unsigned)i;
         nact = (unsigned)na;
+        itime = init ? 0.0 : S.itime;
     } else {
+        if (S.done) {
+            if (threadIdx.x == 0) { S.items = 0; S.bitems = 0; S.nact = 0; }
+            return;
+        }
+        // Hermite4::next_integration_time (Hermite4.cpp:90-102) for this system
+        double m = __longlong_as_double((long long)exact::INF_BITS);
+        for (int i = threadIdx.x; i < n; i += THREADS) m = fmin(m, exact::add(d.t[off + i], d.dt[off + i]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, o));
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        __syncthreads();
+        if (lane == 0) redd[w] = m;
+        __syncthreads();
+        m = redd[0];
+        for (int k = 1; k < WARPS; k++) m = fmin(m, redd[k]);
+        __syncthreads();
+        // the reference's loop condition, on the last step's block time
+        const bool stop = S.err != 0u || !(S.itime < S.t_end);
+        if (stop) {
+            if (threadIdx.x == 0) { S.atime = m; S.done = 1u; S.items = 0; S.bitems = 0; S.nact = 0; }
+            return;
+        }
+        itime = m;
         // ascending compaction, 8 particles per thread per round
         for (int base = 0; base < n; base += THREADS * 8) {
             unsigned flags = 0, cnt = 0;
@@ -194,30 +231,14 @@ __device__ void phase0(const Dev &d, int c, bool init, unsigned *red) {
             nact += tot;
         }
     }
-    // predictor of all particles (init: the state itself, Hermite4::init_data)
-    for (int i = threadIdx.x; i < n; i += THREADS) {
-        const int g = off + i;
-        dbl4 pr, pv;
-        if (init || forced) {
-            pr = d.r[g];
-            pr.w = (double)(float)pr.w;
-            pv = d.v[g];
-            pv.w = 0.0;
-        } else {
-            exact::predict(itime, d.t[g], d.f + 6 * (size_t)g, d.r[g], d.v[g], pr, pv);
-        }
-        d.pr[g] = pr;
-        d.pv[g] = pv;
-        if (MODE == H4_FORCE_MIXED) {
-            float4 a, b, cc;
-            exact::pack_jf(pr, pv, a, b, cc);
-            d.jf0[g] = a;
-            d.jf1[g] = b;
-            d.jf2[g] = cc;
-        }
-    }
     if (threadIdx.x == 0) {
         if (!forced) S.itime = itime;   // a tuning probe leaves the block time alone
+        if (!init && !forced) {
+            S.atime = itime;
+            S.steps += 1;
+            S.psteps += nact;
+            S.inter += (unsigned long long)nact * (unsigned long long)n;
+        }
         S.nact = nact;
         unsigned ig, chunk, split;
         if (MODE == H4_FORCE_EXACT) {
@@ -236,12 +257,72 @@ __device__ void phase0(const Dev &d, int c, bool init, unsigned *red) {
                 split = ((unsigned)n + chunk - 1) / chunk;
             }
         }
+        S.bitems = 0;
+        if (MODE == H4_FORCE_MIXED && S.e2 > 0.0 && nact >= BLOCK_MIN_NACT) {
+            // block-tiled items: 512 active particles x BCHUNK j each
+            unsigned bsplit = ((unsigned)n + BCHUNK - 1) / BCHUNK;
+            const unsigned cap = (unsigned)(S.part_cap / (6ull * nact));
+            unsigned bchunk = BCHUNK;
+            if (bsplit > cap) {
+                bsplit = max(1u, cap);
+                bchunk = ((((unsigned)n + bsplit - 1) / bsplit) + BJT - 1) / BJT * BJT;
+                bsplit = ((unsigned)n + bchunk - 1) / bchunk;
+            }
+            ig = BTI;
+            chunk = bchunk;
+            split = bsplit;
+        }
         S.ig = ig;
         S.chunk = chunk;
         S.split = split;
         S.n_groups = nact ? (nact + ig - 1) / ig : 0;
-        S.items = S.n_groups * split;
+        if (ig == (unsigned)BTI && MODE == H4_FORCE_MIXED) {
+            S.bitems = S.n_groups * split;
+            S.items = 0;
+        } else {
+            S.items = S.n_groups * split;
+        }
     }
+    __syncthreads();
+}
+
+// ---- phase B (grid-wide): predictor of one particle of a stepping system ----
+template <int MODE>
+__device__ __forceinline__ void predict_one(const Dev &d, const System &S, size_t g, bool from_state) {
+    dbl4 pr, pv;
+    if (from_state) {   // Hermite4::init_data predictors (Hermite4.cpp:202-214)
+        pr = d.r[g];
+        pr.w = (double)(float)pr.w;
+        pv = d.v[g];
+        pv.w = 0.0;
+    } else {
+        exact::predict(S.itime, d.t[g], d.f + 6 * g, d.r[g], d.v[g], pr, pv);
+    }
+    d.pr[g] = pr;
+    d.pv[g] = pv;
+    if (MODE == H4_FORCE_MIXED) {
+        float4 a, b, cc;
+        exact::pack_jf(pr, pv, a, b, cc);
+        d.jf0[g] = a;
+        d.jf1[g] = b;
+        d.jf2[g] = cc;
+        const size_t tp = (size_t)d.total;
+        d.jd[g] = make_float4(a.x, a.x, a.y, a.y);
+        d.jd[tp + g] = make_float4(a.z, a.z, a.w, a.w);
+        d.jd[2 * tp + g] = make_float4(b.x, b.x, b.y, b.y);
+        d.jd[3 * tp + g] = make_float4(b.z, b.z, cc.x, cc.x);
+        d.jd[4 * tp + g] = make_float4(cc.y, cc.y, cc.z, cc.z);
+    }
+}
+
+// Last c with pre[c] <= x, over pre[0..m] (pre[0] = 0, nondecreasing).
+__device__ __forceinline__ int find_seg(const unsigned *pre, int m, unsigned x) {
+    int lo = 0, hi = m;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (pre[mid] <= x) lo = mid; else hi = mid;
+    }
+    return lo;
 }
 
 // ---- P1: one warp item of some system's force sum ---------------------------
@@ -297,119 +378,226 @@ __device__ void force_item(const Dev &d, const System &S, unsigned local, int la
     }
 }
 
-// ---- P2: reduction, corrector, timesteps, next time of one system -----------
-__device__ void phase2(const Dev &d, int c, bool init, double *redd) {
-    System &S = d.sys[c];
-    if (S.done) return;
+// ---- P1 (mixed form, large active sets): one block item ---------------------
+// 512 active particles (a packed pair per thread) against a j-chunk that
+// streams through shared memory in tiles of 256; j past the system's end are
+// zero-mass padding (exact zero terms).  Needs e2 > 0 (the self term is then
+// an exact zero).  Sums as k_force_mixed_tiled_x2: FP32 over 64 j, Kahan
+// across, stored as doubles.
+__device__ void block_item(const Dev &d, const System &S, unsigned local, float4 (*sj)[BJT]) {
+    using namespace pair;
+    const unsigned s = local / S.n_groups;
+    const unsigned g = local - s * S.n_groups;
     const int off = S.off, n = S.n;
+    const unsigned nact = S.nact;
+    const int jb = (int)(s * S.chunk);
+    const int je = min(n, jb + (int)S.chunk);
+    const unsigned k0 = g * BTI + threadIdx.x, k1 = k0 + THREADS;
+    const unsigned *move = d.move + off;
+    const float4 *jf0 = d.jf0 + off, *jf1 = d.jf1 + off, *jf2 = d.jf2 + off;
+    const IParticle a = load_i(jf0, jf1, jf2, move[k0 < nact ? k0 : nact - 1]);
+    const IParticle b = load_i(jf0, jf1, jf2, move[k1 < nact ? k1 : nact - 1]);
+    IPair ip;
+    ip.xh = pk2(a.xh, b.xh); ip.yh = pk2(a.yh, b.yh); ip.zh = pk2(a.zh, b.zh);
+    ip.xl = pk2(a.xl, b.xl); ip.yl = pk2(a.yl, b.yl); ip.zl = pk2(a.zl, b.zl);
+    ip.vx = pk2(a.vx, b.vx); ip.vy = pk2(a.vy, b.vy); ip.vz = pk2(a.vz, b.vz);
+    const float e2f = (float)S.e2;
+    const f2 e2 = pk2(e2f, e2f), m3 = pk2(-3.0f, -3.0f);
+    f2 Sum[6], Cmp[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) { Sum[c] = 0ull; Cmp[c] = 0ull; }
+    const size_t tp = (size_t)d.total;
+    for (int j0 = jb; j0 < je; j0 += BJT) {
+        const int j = j0 + (int)threadIdx.x;
+        if (j < je) {
+            const size_t gj = (size_t)off + j;
+#pragma unroll
+            for (int pl = 0; pl < 5; pl++) sj[pl][threadIdx.x] = d.jd[pl * tp + gj];
+        } else {
+            sj[0][threadIdx.x] = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 1.0e15f);
+            sj[1][threadIdx.x] = make_float4(1.0e15f, 1.0e15f, 0.f, 0.f);
+#pragma unroll
+            for (int pl = 2; pl < 5; pl++) sj[pl][threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int sb = 0; sb < BJT; sb += 64) {
+            f2 part[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) part[c] = 0ull;
+#pragma unroll 4
+            for (int jj = sb; jj < sb + 64; jj++) {
+                const f2 *q0 = (const f2 *)&sj[0][jj], *q1 = (const f2 *)&sj[1][jj], *q2 = (const f2 *)&sj[2][jj],
+                         *q3 = (const f2 *)&sj[3][jj], *q4 = (const f2 *)&sj[4][jj];
+                pair_x2(ip, q0[0], q0[1], q1[0], q1[1], q2[0], q2[1], q3[0], q3[1], q4[0], q4[1], e2, m3, part);
+            }
+#pragma unroll
+            for (int c = 0; c < 6; c++) kahan2(Sum[c], Cmp[c], part[c]);
+        }
+        __syncthreads();
+    }
+    double *part_s = d.part + S.part_off + (size_t)s * 6 * nact;
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+        if (k0 < nact) part_s[(size_t)c * nact + k0] = (double)lo2(Sum[c]) - (double)lo2(Cmp[c]);
+        if (k1 < nact) part_s[(size_t)c * nact + k1] = (double)hi2(Sum[c]) - (double)hi2(Cmp[c]);
+    }
+}
+
+// ---- phase D (grid-wide): reduction, corrector and timestep of one active
+// particle (init: forces and the initial timestep) -----------------------------
+__device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k, bool init) {
     const unsigned nact = S.nact, split = S.split;
-    const double itime = S.itime;
-    bool bad = false;
-    for (unsigned k = threadIdx.x; k < nact; k += THREADS) {
-        const unsigned i = d.move[off + k];
-        const size_t g = (size_t)off + i;
-        double fn[6];
+    const unsigned i = d.move[S.off + k];
+    const size_t g = (size_t)S.off + i;
+    double fn[6];
 #pragma unroll
-        for (int q = 0; q < 6; q++) fn[q] = 0.0;
-        for (unsigned s = 0; s < split; s++) {
-            const double *p = d.part + S.part_off + (size_t)s * 6 * nact;
+    for (int q = 0; q < 6; q++) fn[q] = 0.0;
+    for (unsigned s = 0; s < split; s++) {
+        const double *p = d.part + S.part_off + (size_t)s * 6 * nact;
 #pragma unroll
-            for (int q = 0; q < 6; q++) fn[q] = exact::add(fn[q], p[(size_t)q * nact + k]);
-        }
-        double *fp = d.f + 6 * g;
-        if (init) {
-#pragma unroll
-            for (int q = 0; q < 6; q++) fp[q] = fn[q];
-            d.dt[g] = exact::init_dt(fn, (double)0.01f, S.dt_min, S.dt_max);
-            d.t[g] = 0.0;
-            continue;
-        }
-        double o[6];
-        double *op = d.old + 6 * g;
-#pragma unroll
-        for (int q = 0; q < 6; q++) { o[q] = fp[q]; op[q] = o[q]; fp[q] = fn[q]; }
-        dbl4 r = d.r[g], v = d.v[g];
-        double a2[3], a3[3], ndt;
-        const bool ok = exact::correct(itime, S.eta, S.dt_min, S.dt_max, fn, o, d.pr[g], d.pv[g], d.dt[g], r, v,
-                                       a2, a3, ndt);
-        d.r[g] = r;
-        d.v[g] = v;
-#pragma unroll
-        for (int q = 0; q < 3; q++) { d.a2[3 * g + q] = a2[q]; d.a3[3 * g + q] = a3[q]; }
-        d.t[g] = itime;
-        d.dt[g] = ndt;
-        bad |= !ok;
+        for (int q = 0; q < 6; q++) fn[q] = exact::add(fn[q], p[(size_t)q * nact + k]);
     }
-    __syncthreads();
-    // next block time of this system: min (t + dt)
-    double m = __longlong_as_double((long long)exact::INF_BITS);
-    for (int i = threadIdx.x; i < n; i += THREADS) m = fmin(m, exact::add(d.t[off + i], d.dt[off + i]));
+    double *fp = d.f + 6 * g;
+    if (init) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, o));
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) redd[w] = m;
-    const int anybad = __syncthreads_or(bad);
-    if (threadIdx.x == 0) {
-        for (int k = 1; k < WARPS; k++) m = fmin(m, redd[k]);
-        S.atime = m;
-        if (!init) {
-            S.steps += 1;
-            S.psteps += nact;
-            S.inter += (unsigned long long)nact * (unsigned long long)n;
-        }
-        if (anybad) {
-            S.err |= H4_ERRBIT_NONFINITE;
-            atomicOr(d.err, (unsigned)H4_ERRBIT_NONFINITE);
-        }
-        S.done = (anybad || !(itime < S.t_end)) ? 1u : 0u;
-        if (init) S.done = (0.0 < S.t_end) ? 0u : 1u;
+        for (int q = 0; q < 6; q++) fp[q] = fn[q];
+        d.dt[g] = exact::init_dt(fn, (double)0.01f, S.dt_min, S.dt_max);
+        d.t[g] = 0.0;
+        return;
     }
-    __syncthreads();
+    double o[6];
+    double *op = d.old + 6 * g;
+#pragma unroll
+    for (int q = 0; q < 6; q++) { o[q] = fp[q]; op[q] = o[q]; fp[q] = fn[q]; }
+    dbl4 r = d.r[g], v = d.v[g];
+    double a2[3], a3[3], ndt;
+    const bool ok = exact::correct(S.itime, S.eta, S.dt_min, S.dt_max, fn, o, d.pr[g], d.pv[g], d.dt[g], r, v, a2,
+                                   a3, ndt);
+    d.r[g] = r;
+    d.v[g] = v;
+#pragma unroll
+    for (int q = 0; q < 3; q++) { d.a2[3 * g + q] = a2[q]; d.a3[3 * g + q] = a3[q]; }
+    d.t[g] = S.itime;
+    d.dt[g] = ndt;
+    if (!ok) {
+        atomicOr(&S.err, (unsigned)H4_ERRBIT_NONFINITE);
+        atomicOr(d.err, (unsigned)H4_ERRBIT_NONFINITE);
+    }
 }
 
 template <int MODE>
 __global__ void __launch_bounds__(THREADS) k_ensemble(Dev d, int iters, int init, int force_only) {
-    extern __shared__ unsigned s_prefix[];   // [nsys + 1]
+    // per-system prefix sums, [nsys + 1] each: particle offsets, warp items,
+    // block items, active particles
+    extern __shared__ unsigned s_dyn[];
+    unsigned *s_off = s_dyn;
+    unsigned *s_prefix = s_off + d.nsys + 1;
+    unsigned *s_prefix_b = s_prefix + d.nsys + 1;
+    unsigned *s_act = s_prefix_b + d.nsys + 1;
     __shared__ unsigned red[WARPS];
     __shared__ double redd[WARPS];
     __shared__ unsigned s_item[WARPS];
+    __shared__ unsigned s_bitem;
+    __shared__ __align__(16) float4 sj[MODE == H4_FORCE_MIXED ? 5 : 1][BJT];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const bool from_state = init || (*d.forced_nact != 0u);
+    const unsigned nthreads = gridDim.x * THREADS;
+    const unsigned gtid = blockIdx.x * THREADS + threadIdx.x;
     for (int it = 0; it < iters; it++) {
+        // A: per system
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             *d.queue = 0u;
+            *d.queue_b = 0u;
             __threadfence();
         }
-        for (int c = blockIdx.x; c < d.nsys; c += gridDim.x) phase0<MODE>(d, c, init != 0, red);
+        for (int c = blockIdx.x; c < d.nsys; c += gridDim.x) phaseA<MODE>(d, c, init != 0, red, redd);
         if (!grid_sync(d)) return;
-        // prefix of the systems' item counts
-        unsigned carry = 0;
+        // prefix sums of the systems' counts
+        unsigned c_off = 0, c_w = 0, c_b = 0, c_a = 0;
         for (int base = 0; base < d.nsys; base += THREADS) {
             const int c = base + threadIdx.x;
-            const unsigned x = c < d.nsys ? d.sys[c].items : 0u;
-            unsigned tot;
-            const unsigned ex = block_scan_u(x, red, &tot);
-            if (c < d.nsys) s_prefix[c] = carry + ex;
-            carry += tot;
+            const bool v = c < d.nsys;
+            const unsigned x_off = v ? (unsigned)d.sys[c].n : 0u;
+            const unsigned x_w = v ? d.sys[c].items : 0u;
+            const unsigned x_b = v ? d.sys[c].bitems : 0u;
+            const unsigned x_a = v ? d.sys[c].nact : 0u;
+            unsigned t0, t1, t2, t3;
+            const unsigned e0 = block_scan_u(x_off, red, &t0);
+            const unsigned e1 = block_scan_u(x_w, red, &t1);
+            const unsigned e2 = block_scan_u(x_b, red, &t2);
+            const unsigned e3 = block_scan_u(x_a, red, &t3);
+            if (v) {
+                s_off[c] = c_off + e0;
+                s_prefix[c] = c_w + e1;
+                s_prefix_b[c] = c_b + e2;
+                s_act[c] = c_a + e3;
+            }
+            c_off += t0; c_w += t1; c_b += t2; c_a += t3;
         }
-        if (threadIdx.x == 0) s_prefix[d.nsys] = carry;
+        if (threadIdx.x == 0) {
+            s_off[d.nsys] = c_off; s_prefix[d.nsys] = c_w; s_prefix_b[d.nsys] = c_b; s_act[d.nsys] = c_a;
+        }
         __syncthreads();
-        const unsigned total = carry;
+        // B: predictor of every particle of the systems taking a step
+        for (unsigned g = gtid; g < (unsigned)d.total; g += nthreads) {
+            const int c = find_seg(s_off, d.nsys, g);
+            const System &S = d.sys[c];
+            if (S.nact == 0u) continue;
+            predict_one<MODE>(d, S, g, from_state);
+        }
+        if (!grid_sync(d)) return;
+        // C: force sums
+        if (MODE == H4_FORCE_MIXED) {
+            const unsigned total_b = c_b;
+            for (;;) {
+                if (threadIdx.x == 0) s_bitem = atomicAdd(d.queue_b, 1u);
+                __syncthreads();
+                const unsigned item = s_bitem;
+                __syncthreads();
+                if (item >= total_b) break;
+                const int c = find_seg(s_prefix_b, d.nsys, item);
+                block_item(d, d.sys[c], item - s_prefix_b[c], sj);
+            }
+        }
+        const unsigned total = c_w;
         for (;;) {
             if (lane == 0) s_item[w] = atomicAdd(d.queue, 1u);
             __syncwarp();
             const unsigned item = s_item[w];
             __syncwarp();
             if (item >= total) break;
-            int lo = 0, hi = d.nsys;   // last c with s_prefix[c] <= item
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (s_prefix[mid] <= item) lo = mid; else hi = mid;
-            }
-            force_item<MODE>(d, d.sys[lo], item - s_prefix[lo], lane);
+            const int c = find_seg(s_prefix, d.nsys, item);
+            force_item<MODE>(d, d.sys[c], item - s_prefix[c], lane);
         }
         if (!grid_sync(d)) return;
         if (force_only) return;
-        for (int c = blockIdx.x; c < d.nsys; c += gridDim.x) phase2(d, c, init != 0, redd);
+        // D: corrector of every active particle
+        for (unsigned a = gtid; a < c_a; a += nthreads) {
+            const int c = find_seg(s_act, d.nsys, a);
+            correct_one(d, d.sys[c], a - s_act[c], init != 0);
+        }
+        if (!grid_sync(d)) return;
+        if (init) {
+            // Hermite4::init_dt's CTIME and the first loop condition
+            for (int c = blockIdx.x; c < d.nsys; c += gridDim.x) {
+                System &S = d.sys[c];
+                double m = __longlong_as_double((long long)exact::INF_BITS);
+                for (int i = threadIdx.x; i < S.n; i += THREADS) m = fmin(m, d.dt[S.off + i]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, o));
+                __syncthreads();
+                if (lane == 0) redd[w] = m;
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    for (int k = 1; k < WARPS; k++) m = fmin(m, redd[k]);
+                    S.atime = m;
+                    S.itime = 0.0;
+                    S.done = (0.0 < S.t_end) ? 0u : 1u;
+                }
+                __syncthreads();
+            }
+        }
     }
 }
 
@@ -653,7 +841,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
                   const h4_double4 *r, const h4_double4 *v, int mode) {
     if (!out) return efail(H4_ERR_ARG, "h4_ens_create: out is NULL");
     *out = nullptr;
-    if (nsys < 1 || nsys > MAX_SYSTEMS) return efail(H4_ERR_ARG, "h4_ens_create: nsys must be in [1, 8192]");
+    if (nsys < 1 || nsys > MAX_SYSTEMS) return efail(H4_ERR_ARG, "h4_ens_create: nsys must be in [1, 4096]");
     if (!n || !e2 || !eta || !r || !v) return efail(H4_ERR_ARG, "h4_ens_create: null array");
     if (mode < H4_FORCE_FP64 || mode > H4_FORCE_MIXED) return efail(H4_ERR_ARG, "h4_ens_create: unknown mode");
     size_t total = 0, part_total = 0;
@@ -703,10 +891,10 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     EA(d.sys, nsys); EA(d.r, total); EA(d.v, total); EA(d.pr, total); EA(d.pv, total);
     EA(d.f, 6 * total); EA(d.old, 6 * total); EA(d.a2, 3 * total); EA(d.a3, 3 * total);
     EA(d.t, total); EA(d.dt, total); EA(d.move, total); EA(d.part, part_total);
-    EA(d.queue, 1); EA(d.bar_count, 1); EA(d.bar_gen, 1); EA(d.err, 1);
+    EA(d.queue, 1); EA(d.queue_b, 1); EA(d.bar_count, 1); EA(d.bar_gen, 1); EA(d.err, 1);
     EA(d.tune_ig, NB_N * NB_A); EA(d.tune_chunk, NB_N * NB_A); EA(d.forced_nact, 1); EA(d.launches, 1);
     EA(d.epot_i, total); EA(d.energy, 2 * nsys);
-    if (mode == H4_FORCE_MIXED) { EA(d.jf0, total); EA(d.jf1, total); EA(d.jf2, total); }
+    if (mode == H4_FORCE_MIXED) { EA(d.jf0, total); EA(d.jf1, total); EA(d.jf2, total); EA(d.jd, 5 * total); }
 #undef EA
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->own, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&E->e0);
@@ -727,13 +915,14 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     size_t zb[] = {48 * total, 48 * total, 24 * total, 24 * total, 8 * total, 8 * total};
     for (int k = 0; k < 6 && e == cudaSuccess; k++) e = cudaMemsetAsync(zero[k], 0, zb[k], s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.queue, 0, 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.queue_b, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.bar_count, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.bar_gen, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.err, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.forced_nact, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.launches, 0, 8, s);
     // persistent grid: every block resident (cooperative launch)
-    E->smem = sizeof(unsigned) * (nsys + 1);
+    E->smem = sizeof(unsigned) * 4 * (nsys + 1);
     int per_sm = 0;
     if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel_for(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel_for(mode), THREADS, E->smem);

@@ -225,84 +225,17 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled(H4Dev d, unsigned t
 // operands.  Same arithmetic per lane as pair_mixed (and hence the same
 // results up to the order of the FP32 partial sums, which is identical here).
 
-typedef unsigned long long f2;
+using pair::f2;
+using pair::pk2;
+using pair::lo2;
+using pair::hi2;
+using pair::IPair;
+using pair::kahan2;
+using pair::pair_x2;
 
-__device__ __forceinline__ f2 pk2(float a, float b) {
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ float lo2(f2 v) {
-    float a, b;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-    return a;
-}
-__device__ __forceinline__ float hi2(f2 v) {
-    float a, b;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-    return b;
-}
-__device__ __forceinline__ f2 add2(f2 a, f2 b) {
-    f2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
-    f2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
-    f2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-    f2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-__device__ __forceinline__ f2 rsqrt2(f2 v) {
-    float a, b, ra, rb;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(ra) : "f"(a));
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rb) : "f"(b));
-    return pk2(ra, rb);
-}
 // 128-bit shared load as two packed operands
 __device__ __forceinline__ void lds2(const float4 *p, f2 &a, f2 &b) {
     asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(smem_addr(p)));
-}
-
-struct IPair {   // two active particles, packed
-    f2 xh, yh, zh, xl, yl, zl, vx, vy, vz;
-};
-
-__device__ __forceinline__ void kahan2(f2 &s, f2 &c, f2 x) {
-    const f2 y = sub2(x, c);
-    const f2 t = add2(s, y);
-    c = sub2(sub2(t, s), y);
-    s = t;
-}
-
-__device__ __forceinline__ void pair_x2(const IPair &p, f2 jxh, f2 jyh, f2 jzh, f2 jm, f2 jxl, f2 jyl, f2 jzl,
-                                        f2 jvx, f2 jvy, f2 jvz, f2 e2, f2 m3, f2 sum[6]) {
-    const f2 dx = add2(sub2(jxh, p.xh), sub2(jxl, p.xl));
-    const f2 dy = add2(sub2(jyh, p.yh), sub2(jyl, p.yl));
-    const f2 dz = add2(sub2(jzh, p.zh), sub2(jzl, p.zl));
-    const f2 dvx = sub2(jvx, p.vx), dvy = sub2(jvy, p.vy), dvz = sub2(jvz, p.vz);
-    const f2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-    const f2 rinv = rsqrt2(r2);
-    const f2 r2inv = mul2(rinv, rinv);
-    const f2 A = mul2(mul2(jm, rinv), r2inv);
-    const f2 rv = fma2(dx, dvx, fma2(dy, dvy, mul2(dz, dvz)));
-    const f2 eta = mul2(rv, mul2(m3, r2inv));
-    sum[0] = fma2(A, dx, sum[0]);
-    sum[1] = fma2(A, dy, sum[1]);
-    sum[2] = fma2(A, dz, sum[2]);
-    sum[3] = fma2(A, fma2(eta, dx, dvx), sum[3]);
-    sum[4] = fma2(A, fma2(eta, dy, dvy), sum[4]);
-    sum[5] = fma2(A, fma2(eta, dz, dvz), sum[5]);
 }
 
 constexpr int IPT2 = 4;            // active particles per thread (2 packed pairs)

@@ -124,3 +124,21 @@ def test_ensemble_energy_matches_oracle():
         e, k, pp = o.energy()
         assert abs(ek[c] - k) <= 1e-12 * abs(k)
         assert abs(ep[c] - pp) <= 1e-12 * max(abs(pp), 1e-300)
+
+
+def test_ensemble_mixed_forces_vs_oracle():
+    """Initial forces of every system (all particles active: block-tiled items
+    for N >= 512, warp items below) within the mixed-form tolerance."""
+    from h4_util import rel_err_vec
+    systems = _systems([300, 700, 2048, 5000], seed0=1100)
+    with Ensemble(systems, mode="mixed") as E:
+        E.init()
+        f = E.download()["f"]
+    for c, (m, p, v, soft, eta) in enumerate(systems):
+        want = orc.forces_for(orc.make_predictors(m, p, v), orc.e2_from_softening(soft),
+                              np.arange(len(m), dtype=np.uint32))
+        got = f[E.system_slice(c)]
+        ea = rel_err_vec(got[:, :3], want[:, :3])
+        ej = rel_err_vec(got[:, 3:], want[:, 3:])
+        assert np.median(ea) < 1e-6 and ea.max() < 1e-4, (c, np.median(ea), ea.max())
+        assert np.median(ej) < 1e-6 and ej.max() < 1e-3, (c, np.median(ej), ej.max())
