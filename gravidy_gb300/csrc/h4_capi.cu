@@ -36,6 +36,11 @@ int cuda_fail(cudaError_t e, const char *what) {
         if (e__ != cudaSuccess) return cuda_fail(e__, what); \
     } while (0)
 
+// Active-set size from which the tiled mixed kernel beats the warp items
+// (measured on GB300: at N = 65536 the tiled kernel is faster from N_act ~ 64,
+// at N = 16384 from ~ 256).
+unsigned default_mixed_threshold(unsigned n) { return n >= 32768u ? 64u : 256u; }
+
 bool is_pow2(double x) {
     if (!(x > 0.0) || !std::isfinite(x)) return false;
     int ex;
@@ -62,7 +67,7 @@ struct h4_system_s {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_mode = -1;
-    unsigned mixed_threshold = MIXED_TILED_THRESHOLD_DEFAULT;
+    unsigned mixed_threshold = 0;   // set at creation from N
     cudaStream_t graph_stream = nullptr;
 };
 
@@ -214,6 +219,7 @@ int h4_create(h4_handle *out, unsigned int n, double e2, float eta, const h4_dou
     d.dt_min = 1.1920928955078125e-07;
     d.dt_max = 0.125;
     h->mode = mode;
+    h->mixed_threshold = default_mixed_threshold(n);
     const size_t N = n, NP = (size_t)d.n_pad;
     d.part_cap = 6 * (N + 262144);
     const int nflag = (int)((N + FLAG_CHUNK - 1) / FLAG_CHUNK);

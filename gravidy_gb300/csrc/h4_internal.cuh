@@ -101,7 +101,7 @@ void launch_force_fp64(const H4Dev &d, int grid_warps, cudaStream_t s);
 void launch_force_exact(const H4Dev &d, cudaStream_t s);   // writes d.part with S = 1
 // Returns the number of kernels launched (1 or 2).
 int launch_force_mixed(const H4Dev &d, int num_sms, unsigned threshold, long long known_nact, cudaStream_t s);
-constexpr unsigned MIXED_TILED_THRESHOLD_DEFAULT = 4096;
+
 int force_fp64_grid_warps(int num_sms);
 
 // ---- energy (h4_energy.cu) --------------------------------------------------

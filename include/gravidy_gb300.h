@@ -87,7 +87,7 @@ int h4_set_dt_limits(h4_handle h, double dt_min, double dt_max);
 int h4_set_force_mode(h4_handle h, int mode);
 /* H4_FORCE_MIXED: active-set size from which the shared-memory tiled kernel
  * (lanes over active particles) is used instead of warp items (lanes over j).
- * Default 4096; the autotuner picks it per (N, N_act) bucket. */
+ * Default 64 for N >= 32768, else 256 (measured crossover on GB300). */
 int h4_set_mixed_threshold(h4_handle h, unsigned int nact_threshold);
 
 /* Hermite4GPU::init_acc_jrk (Hermite4GPU.cu:333-375): acc and jerk of all
