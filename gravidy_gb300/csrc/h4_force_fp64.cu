@@ -31,8 +31,14 @@
 namespace h4 {
 namespace {
 
+#ifndef H4_FP64_IG
+#define H4_FP64_IG 4
+#endif
+#ifndef H4_FP64_BPS
+#define H4_FP64_BPS 2
+#endif
 constexpr int WARPS = 4;        // warps per block
-constexpr int IG = 4;           // active particles per work item
+constexpr int IG = H4_FP64_IG;  // active particles per work item (build knob: 2, 4 or 8)
 constexpr int ITEMS_PER_WARP = 12;
 
 __global__ void __launch_bounds__(WARPS * 32) k_force_fp64(H4Dev d) {
@@ -69,15 +75,19 @@ __global__ void __launch_bounds__(WARPS * 32) k_force_fp64(H4Dev d) {
         const unsigned k0 = g * IG;
         const unsigned cnt = min((unsigned)IG, nact - k0);
         double *part_s = d.part + (size_t)s * 6 * nact;
-        if (cnt == 4) {
-            pair::fp64_warp_item<4>(d.pr, d.pv, d.move, nact, k0, j_begin, j_end, d.e2, part_s, lane);
+        if (cnt == (unsigned)IG) {
+            pair::fp64_warp_item<IG>(d.pr, d.pv, d.move, nact, k0, j_begin, j_end, d.e2, part_s, lane);
         } else {
-            unsigned k = k0;
-            if (cnt >= 2) {
-                pair::fp64_warp_item<2>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
-                k += 2;
+            unsigned k = k0, left = cnt;
+            if (IG > 4 && left >= 4) {
+                pair::fp64_warp_item<4>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
+                k += 4; left -= 4;
             }
-            if (cnt & 1) pair::fp64_warp_item<1>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
+            if (left >= 2) {
+                pair::fp64_warp_item<2>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
+                k += 2; left -= 2;
+            }
+            if (left & 1) pair::fp64_warp_item<1>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
         }
     }
 }
@@ -98,7 +108,7 @@ __global__ void __launch_bounds__(128) k_force_exact(H4Dev d) {
 
 }  // namespace
 
-int force_fp64_grid_warps(int num_sms) { return num_sms * 2 * WARPS; }
+int force_fp64_grid_warps(int num_sms) { return num_sms * H4_FP64_BPS * WARPS; }
 
 void launch_force_fp64(const H4Dev &d, int grid_warps, cudaStream_t s) {
     int blocks = grid_warps / WARPS;

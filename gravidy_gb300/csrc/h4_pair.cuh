@@ -9,8 +9,15 @@
 #pragma once
 #include "h4_internal.cuh"
 
+// j-loop unroll of the FP64 warp items (a build knob; 1 = as measured).
+#ifndef H4_FP64_JUNROLL
+#define H4_FP64_JUNROLL 1
+#endif
+
 namespace h4 {
 namespace pair {
+
+constexpr int kFp64JUnroll = H4_FP64_JUNROLL;
 
 // 1/sqrt(x) in FP64: hardware reciprocal-square-root approximation
 // (rsqrt.approx.f64) refined by one cubic Householder step,
@@ -63,6 +70,7 @@ __device__ __forceinline__ void fp64_warp_item(const dbl4 *__restrict__ pr, cons
 #pragma unroll
         for (int c = 0; c < 6; c++) acc[q][c] = 0.0;
     }
+#pragma unroll kFp64JUnroll
     for (int j = j_begin + lane; j < j_end; j += 32) {
         const dbl4 pj = pr[j], vj = pv[j];
 #pragma unroll
