@@ -52,6 +52,7 @@ SIGNATURES = {
     "h4_kernel_launches": (_i, [_vp, C.POINTER(C.c_ulonglong)]),
     "h4_nact_histogram": (_i, [_vp, _vp]),
     "h4_probe_peaks": (_i, [_pd, _pd]),
+    "h4_selftest_bounded_wait": (_i, [_d, C.POINTER(_i)]),
     "h4_forces_noalloc": (_i, [_u, _d, _vp, _vp, _u, _vp, _vp, _vp]),
     "h4_center_of_density": (_i, [_vp, _vp]),
     "h4_mass_radii": (_i, [_vp, _vp, _f, _pd, _pd, _vp]),

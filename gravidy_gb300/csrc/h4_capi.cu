@@ -642,6 +642,14 @@ int h4_kernel_launches(h4_handle h, unsigned long long *count) {
     return H4_OK;
 }
 
+int h4_selftest_bounded_wait(double seconds, int *timed_out) {
+    if (!(seconds > 0.0) || seconds > 5.0 || !timed_out)
+        return fail(H4_ERR_ARG, "h4_selftest_bounded_wait: seconds in (0, 5], timed_out not NULL");
+    cudaError_t e = selftest_bounded_wait(seconds, timed_out);
+    if (e != cudaSuccess) return cuda_fail(e, "h4_selftest_bounded_wait");
+    return H4_OK;
+}
+
 int h4_probe_peaks(double *fp64_flops, double *fp32_flops) {
     cudaError_t e = probe_peaks(fp64_flops, fp32_flops);
     if (e != cudaSuccess) return cuda_fail(e, "h4_probe_peaks");

@@ -87,12 +87,6 @@ struct Dev {
     int mode;
 };
 
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 // Grid-wide barrier of a cooperative launch, bounded in time.
 __device__ bool grid_sync(const Dev &d) {
     __syncthreads();
@@ -105,15 +99,8 @@ __device__ bool grid_sync(const Dev &d) {
             *d.bar_count = 0u;
             __threadfence();
             atomicAdd((unsigned *)d.bar_gen, 1u);
-        } else {
-            const unsigned long long t0 = global_ns();
-            while (*gen == g0) {
-                if (global_ns() - t0 > BARRIER_TIMEOUT_NS) {
-                    atomicOr(d.err, (unsigned)H4_ERRBIT_TIMEOUT);
-                    break;
-                }
-                __nanosleep(100);
-            }
+        } else if (!bounded_wait_change(gen, g0, BARRIER_TIMEOUT_NS)) {
+            atomicOr(d.err, (unsigned)H4_ERRBIT_TIMEOUT);
         }
         __threadfence();
     }
@@ -612,7 +599,9 @@ __global__ void k_ens_check(Dev d, cudaGraphConditionalHandle cond) {
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned long long l = ++*d.launches;
-        unsigned go = any && (*d.err == 0u);
+        // a system that went non-finite stops alone (phase A); a timed-out
+        // barrier or the launch bound stops everything
+        unsigned go = any && ((*d.err & (H4_ERRBIT_TIMEOUT | H4_ERRBIT_STEPCAP)) == 0u);
         if (go && l >= d.max_launches) {
             atomicOr(d.err, (unsigned)H4_ERRBIT_STEPCAP);
             go = 0;

@@ -47,6 +47,26 @@ enum : unsigned int {
     H4_ERRBIT_TIMEOUT = 8u,        // a bounded wait (mbarrier) gave up
 };
 
+// Device clock in ns (%globaltimer).
+__device__ __forceinline__ unsigned long long device_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits until *word differs from `old`, for at most timeout_ns; false on
+// timeout.  Every inter-block wait of this library goes through here, so no
+// wait can run forever: the caller records an error bit and returns.
+__device__ __forceinline__ bool bounded_wait_change(const volatile unsigned *word, unsigned old,
+                                                    unsigned long long timeout_ns) {
+    const unsigned long long t0 = device_ns();
+    while (*word == old) {
+        if (device_ns() - t0 > timeout_ns) return false;
+        __nanosleep(100);
+    }
+    return true;
+}
+
 struct H4Dev {
     int n;          // particles
     int n_pad;      // predicted arrays are padded to a multiple of 256
@@ -109,5 +129,6 @@ void launch_energy(const H4Dev &d, cudaStream_t s);
 
 // ---- peaks -------------------------------------------------------------------
 cudaError_t probe_peaks(double *fp64, double *fp32);
+cudaError_t selftest_bounded_wait(double seconds, int *timed_out);
 
 }  // namespace h4

@@ -36,6 +36,28 @@ __global__ void k_probe_ffma(float *out, int iters, float a, float b) {
 }
 }  // namespace
 
+// One thread waits, bounded, on a flag that nothing sets.
+__global__ void k_selftest_wait(const unsigned *flag, unsigned long long timeout_ns, unsigned *result) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    *result = bounded_wait_change(flag, 0u, timeout_ns) ? 0u : 1u;
+}
+
+cudaError_t selftest_bounded_wait(double seconds, int *timed_out) {
+    unsigned *buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, 2 * sizeof(unsigned));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(buf, 0, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) {
+        k_selftest_wait<<<1, 32>>>(buf, (unsigned long long)(seconds * 1e9), buf + 1);
+        e = cudaGetLastError();
+    }
+    unsigned r = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&r, buf + 1, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e == cudaSuccess && timed_out) *timed_out = (int)r;
+    return e;
+}
+
 cudaError_t probe_peaks(double *fp64, double *fp32) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);

@@ -272,6 +272,12 @@ int h4_nact_histogram(h4_handle h, unsigned long long counts[32]);
 /* Kernels launched by this handle since creation. */
 int h4_kernel_launches(h4_handle h, unsigned long long *count);
 
+/* Self-test of the bounded device wait every inter-block wait of this library
+ * uses (ensemble grid barriers): one thread waits on a flag that nothing sets,
+ * for `seconds` (<= 5); *timed_out = 1 when the wait gave up as designed.
+ * The context stays usable. */
+int h4_selftest_bounded_wait(double seconds, int *timed_out);
+
 /* Throughput of the FP64 and FP32 pipes on this GPU (flop/s, FMA = 2),
  * measured with a short dependent-FMA kernel; used as roofline peaks. */
 int h4_probe_peaks(double *fp64_flops, double *fp32_flops);
