@@ -40,11 +40,12 @@ Hermite4GB300::~Hermite4GB300() { h4_destroy(h_); }
 void Hermite4GB300::init_acc_jrk() { check(h4_init_acc_jrk(h_), "init_acc_jrk"); }
 
 void Hermite4GB300::update_acc_jrk(int nact) {
-    const double t0 = omp_get_wtime();
+    // the log's GFLOPS column divides by the accumulated update time
+    // (Logger.cpp:333-335); here the force kernel's device time
     check(h4_update_acc_jrk(h_, (unsigned)nact), "update_acc_jrk");
     float ms = 0.f;
     check(h4_last_timings(h_, &ms, 0), "update_acc_jrk");
-    ns->gtime.update_end += (float)(omp_get_wtime() - t0);
+    ns->gtime.update_end += ms * 1e-3f;
 }
 
 void Hermite4GB300::predicted_pos_vel(double ITIME) { check(h4_predicted_pos_vel(h_, ITIME), "predicted_pos_vel"); }
