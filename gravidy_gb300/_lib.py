@@ -26,6 +26,7 @@ SIGNATURES = {
     "h4_last_error": (C.c_char_p, []),
     "h4_status_string": (C.c_char_p, [_i]),
     "h4_abi_version": (_i, []),
+    "h4_build_flags": (_i, []),
     "h4_create": (_i, [C.POINTER(_vp), _u, _d, _f, _vp, _vp, _i]),
     "h4_destroy": (_i, [_vp]),
     "h4_set_stream": (_i, [_vp, _vp]),
@@ -51,6 +52,8 @@ SIGNATURES = {
     "h4_last_timings": (_i, [_vp, C.POINTER(_f), C.POINTER(_f)]),
     "h4_kernel_launches": (_i, [_vp, C.POINTER(C.c_ulonglong)]),
     "h4_nact_histogram": (_i, [_vp, _vp]),
+    "h4_phase_times": (_i, [_vp, _vp, _vp]),
+    "h4_phase_name": (C.c_char_p, [_i]),
     "h4_probe_peaks": (_i, [_pd, _pd]),
     "h4_selftest_bounded_wait": (_i, [_d, C.POINTER(_i)]),
     "h4_forces_noalloc": (_i, [_u, _d, _vp, _vp, _u, _vp, _vp, _vp]),
@@ -83,16 +86,23 @@ class H4Error(RuntimeError):
 _lib = None
 
 
+def library_path() -> str:
+    """The library to load: GRAVIDY_GB300_LIB if set (e.g. the bounds-checked
+    build), else the in-tree build."""
+    return os.environ.get("GRAVIDY_GB300_LIB") or LIB
+
+
 def load(build_if_missing: bool = True):
     """Load the native library (building it first if it is absent)."""
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB):
-        if not build_if_missing:
-            raise OSError(f"{LIB} not built; run python -m gravidy_gb300.build")
+    path = library_path()
+    if not os.path.exists(path):
+        if path != LIB or not build_if_missing:
+            raise OSError(f"{path} not built; run python -m gravidy_gb300.build")
         build_library()
-    L = C.CDLL(LIB)
+    L = C.CDLL(path)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(L, name)
         fn.restype = res

@@ -5,6 +5,11 @@
   (``-gencode arch=compute_103a,code=sm_103a``), one nvcc process per
   translation unit, in parallel, then linked with nvcc.
 * ``gravidy-gb300``: the command-line program (C++ host code over the C ABI).
+* ``bounds/libgravidy_gb300.so`` (``build_library(bounds_check=True)``, or
+  ``python -m gravidy_gb300.build --bounds-check``): the same library with
+  ``-DH4_BOUNDS_CHECK``, whose kernels check every index range they touch
+  and report a violation instead of making the access.  Loaded in place of
+  the normal library when GRAVIDY_GB300_LIB names it.
 
 Outputs go to gravidy_gb300/_build/ (git-ignored).  ``python -m
 gravidy_gb300.build`` runs it.
@@ -24,6 +29,7 @@ HOSTSRC = os.path.join(CSRC, "host")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libgravidy_gb300.so")
 CLI = os.path.join(BUILD, "gravidy-gb300")
+BOUNDS_LIB = os.path.join(BUILD, "bounds", "libgravidy_gb300.so")
 
 CUDA_SOURCES = ["h4_capi.cu", "h4_step_kernels.cu", "h4_force_fp64.cu", "h4_energy.cu", "h4_probe.cu",
                 "h4_noalloc.cu", "h4_force_mixed.cu", "h4_ensemble.cu", "h4_diagnostics.cu"]
@@ -54,8 +60,11 @@ def _stale(target, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build_library(force: bool = False, verbose: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build_library(force: bool = False, verbose: bool = False, bounds_check: bool = False) -> str:
+    out_dir = os.path.dirname(BOUNDS_LIB) if bounds_check else BUILD
+    lib = BOUNDS_LIB if bounds_check else LIB
+    flags = NVCC_FLAGS + (["-DH4_BOUNDS_CHECK"] if bounds_check else [])
+    os.makedirs(out_dir, exist_ok=True)
     nv = nvcc()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "gravidy_gb300.h"))
@@ -63,17 +72,17 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     objs = []
     for src in CUDA_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(out_dir, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nv, *ARCH, *NVCC_FLAGS, "-c", s, "-o", o])
+            jobs.append([nv, *ARCH, *flags, "-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         for out in ex.map(_run, jobs):
             if verbose and out:
                 print(out)
-    if force or jobs or _stale(LIB, objs):
-        _run([nv, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
-    return LIB
+    if force or jobs or _stale(lib, objs):
+        _run([nv, *ARCH, "-shared", "-o", lib, *objs, "-lcudart"])
+    return lib
 
 
 def build_cli(force: bool = False) -> str | None:
@@ -95,5 +104,8 @@ def build_all(force: bool = False, verbose: bool = False) -> None:
 
 
 if __name__ == "__main__":
-    build_all(force="--force" in sys.argv, verbose="-v" in sys.argv)
-    print(LIB)
+    if "--bounds-check" in sys.argv:
+        print(build_library(force="--force" in sys.argv, verbose="-v" in sys.argv, bounds_check=True))
+    else:
+        build_all(force="--force" in sys.argv, verbose="-v" in sys.argv)
+        print(LIB)

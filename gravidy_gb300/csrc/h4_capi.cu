@@ -39,7 +39,10 @@ int cuda_fail(cudaError_t e, const char *what) {
 // Active-set size from which the tiled mixed kernel beats the warp items
 // (measured on GB300: at N = 65536 the tiled kernel is faster from N_act ~ 64,
 // at N = 16384 from ~ 256).
-unsigned default_mixed_threshold(unsigned n) { return n >= 32768u ? 64u : 256u; }
+// Measured crossover of the two mixed kernels on GB300 (force kernel time,
+// N = 32768 .. 2^20): the warp items win below about 1000 active particles at
+// N = 32768, 450 at N = 65536 and 300-330 at N = 262144 and 2^20.
+unsigned default_mixed_threshold(unsigned n) { return n >= 65536u ? 384u : 768u; }
 
 bool is_pow2(double x) {
     if (!(x > 0.0) || !std::isfinite(x)) return false;
@@ -49,6 +52,19 @@ bool is_pow2(double x) {
 }
 
 }  // namespace
+
+// CUDA-event timers per phase, with the reference's phase names (Gtime,
+// src/include/common.hpp:287-310): each phase keeps one pending event pair,
+// resolved when the phase is issued again or when the totals are read.
+enum Phase { PH_PREDICTION, PH_UPDATE, PH_GRAV, PH_CORRECTION, PH_ACTIVE, PH_NEXT, PH_ENERGY, PH_ADVANCE, PH_COUNT };
+static const char *kPhaseNames[PH_COUNT] = {"prediction", "update", "grav", "correction", "active_set",
+                                            "next_time", "energy", "advance"};
+struct PhaseTimer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    bool pending = false;
+    double total_ms = 0.0;
+    unsigned long long count = 0;
+};
 
 struct h4_system_s {
     H4Dev d;
@@ -68,6 +84,7 @@ struct h4_system_s {
     cudaGraphExec_t graph_exec = nullptr;
     int graph_mode = -1;
     unsigned mixed_threshold = 0;   // set at creation from N
+    PhaseTimer phase[PH_COUNT];
     cudaStream_t graph_stream = nullptr;
 };
 
@@ -89,6 +106,33 @@ void free_device(h4_system_s *h) {
     if (h->ev2) cudaEventDestroy(h->ev2);
     if (h->ev3) cudaEventDestroy(h->ev3);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    for (auto &p : h->phase) {
+        if (p.a) cudaEventDestroy(p.a);
+        if (p.b) cudaEventDestroy(p.b);
+    }
+}
+
+void phase_resolve(PhaseTimer &p) {
+    if (!p.pending) return;
+    if (cudaEventSynchronize(p.b) == cudaSuccess) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) p.total_ms += ms;
+        p.count += 1;
+    }
+    p.pending = false;
+}
+
+void phase_begin(h4_system_s *h, Phase ph) {
+    PhaseTimer &p = h->phase[ph];
+    phase_resolve(p);
+    if (!p.a) { cudaEventCreate(&p.a); cudaEventCreate(&p.b); }
+    cudaEventRecord(p.a, h->stream);
+}
+
+void phase_end(h4_system_s *h, Phase ph) {
+    PhaseTimer &p = h->phase[ph];
+    cudaEventRecord(p.b, h->stream);
+    p.pending = true;
 }
 
 int grid_warps(const h4_system_s *h) { return force_fp64_grid_warps(h->num_sms); }
@@ -115,6 +159,8 @@ int sync_ctrl(h4_system_s *h) {
     H4_TRY(cudaMemcpyAsync(h->h_ctrl, h->d.ctrl, sizeof(H4Ctrl), cudaMemcpyDeviceToHost, h->stream),
            "copy control block");
     H4_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    if (h->h_ctrl->err & H4_ERRBIT_BOUNDS)   // bounds-checked build only
+        return fail(H4_ERR_STATE, "bounds check failed at site " + std::to_string(h->h_ctrl->bounds_site));
     return H4_OK;
 }
 
@@ -189,6 +235,8 @@ const char *h4_status_string(int status) {
 }
 
 int h4_abi_version(void) { return H4_ABI_VERSION; }
+
+int h4_build_flags(void) { return kBoundsCheck ? H4_BUILD_BOUNDS_CHECK : 0; }
 
 int h4_create(h4_handle *out, unsigned int n, double e2, float eta, const h4_double4 *r,
               const h4_double4 *v, int mode) {
@@ -359,7 +407,9 @@ int h4_init_dt(h4_handle h, double *atime, float eta, double itime) {
 
 int h4_find_particles_to_move(h4_handle h, double itime, unsigned int *nact) {
     if (!h) return fail(H4_ERR_ARG, "null handle");
+    phase_begin(h, PH_ACTIVE);
     launch_find_active(h->d, true, itime, h->stream);
+    phase_end(h, PH_ACTIVE);
     h->launches += 2;
     int st = check_launch("h4_find_particles_to_move");
     if (st) return st;
@@ -388,7 +438,9 @@ int h4_save_old_acc_jrk(h4_handle h, unsigned int nact) {
 
 int h4_predicted_pos_vel(h4_handle h, double itime) {
     if (!h) return fail(H4_ERR_ARG, "null handle");
+    phase_begin(h, PH_PREDICTION);
     launch_predict(h->d, true, itime, h->stream);
+    phase_end(h, PH_PREDICTION);
     h->launches += 1;
     return check_launch("h4_predicted_pos_vel");
 }
@@ -398,10 +450,14 @@ int h4_update_acc_jrk(h4_handle h, unsigned int nact) {
     int st = set_nact(h, nact);
     if (st) return st;
     if (nact == 0) return H4_OK;
+    phase_begin(h, PH_UPDATE);
+    phase_begin(h, PH_GRAV);
     cudaEventRecord(h->ev0, h->stream);
     launch_force(h, h->stream, (long long)nact);
     cudaEventRecord(h->ev1, h->stream);
+    phase_end(h, PH_GRAV);
     launch_reduce_forces(h->d, false, h->stream);
+    phase_end(h, PH_UPDATE);
     h->launches += 1;
     return check_launch("h4_update_acc_jrk");
 }
@@ -410,14 +466,18 @@ int h4_correction_pos_vel(h4_handle h, double itime, unsigned int nact) {
     if (!h) return fail(H4_ERR_ARG, "null handle");
     int st = set_nact(h, nact);
     if (st) return st;
+    phase_begin(h, PH_CORRECTION);
     launch_correct(h->d, true, itime, false, h->stream);
+    phase_end(h, PH_CORRECTION);
     h->launches += 1;
     return check_launch("h4_correction_pos_vel");
 }
 
 int h4_next_integration_time(h4_handle h, double *atime) {
     if (!h || !atime) return fail(H4_ERR_ARG, "h4_next_integration_time: null argument");
+    phase_begin(h, PH_NEXT);
     launch_next_time(h->d, true, h->stream);
+    phase_end(h, PH_NEXT);
     h->launches += 2;
     int st = check_launch("h4_next_integration_time");
     if (st) return st;
@@ -428,7 +488,9 @@ int h4_next_integration_time(h4_handle h, double *atime) {
 
 int h4_get_energy(h4_handle h, double *ekin, double *epot, double *etot) {
     if (!h) return fail(H4_ERR_ARG, "null handle");
+    phase_begin(h, PH_ENERGY);
     launch_energy(h->d, h->stream);
+    phase_end(h, PH_ENERGY);
     h->launches += 2;
     int st = check_launch("h4_get_energy");
     if (st) return st;
@@ -487,6 +549,8 @@ int h4_advance(h4_handle h, double t_stop, double t_log, double *atime, double *
     cudaEventRecord(h->ev3, s);
     if ((st = sync_ctrl(h))) return st;
     cudaEventElapsedTime(&h->last_advance_ms, h->ev2, h->ev3);
+    h->phase[PH_ADVANCE].total_ms += h->last_advance_ms;
+    h->phase[PH_ADVANCE].count += 1;
     const H4Ctrl &o = *h->h_ctrl;
     h->launches += (unsigned long long)o.steps * (unsigned long long)(step_kernel_count(h) + 1);
     if (atime) *atime = bits_to_double_host(o.atime_bits);
@@ -507,6 +571,10 @@ int h4_advance(h4_handle h, double t_stop, double t_log, double *atime, double *
 int h4_download(h4_handle h, h4_double4 *r, h4_double4 *v, h4_forces *f, h4_forces *old, h4_double3 *a2,
                 h4_double3 *a3, double *t, double *dt, unsigned int *move) {
     if (!h) return fail(H4_ERR_ARG, "null handle");
+    if (kBoundsCheck) {   // a failed check of the bounds-checked build surfaces here at the latest
+        int st = sync_ctrl(h);
+        if (st) return st;
+    }
     const size_t N = h->d.n;
     cudaStream_t s = h->stream;
     if (r) H4_TRY(cudaMemcpyAsync(r, h->d.r, N * 32, cudaMemcpyDeviceToHost, s), "download r");
@@ -634,6 +702,20 @@ int h4_nact_histogram(h4_handle h, unsigned long long counts[32]) {
     if (st) return st;
     for (int k = 0; k < 32; k++) counts[k] = h->h_ctrl->nact_hist[k];
     return H4_OK;
+}
+
+int h4_phase_times(h4_handle h, double ms[H4_PHASES], unsigned long long counts[H4_PHASES]) {
+    if (!h) return fail(H4_ERR_ARG, "null handle");
+    for (int p = 0; p < PH_COUNT; p++) {
+        phase_resolve(h->phase[p]);
+        if (ms) ms[p] = h->phase[p].total_ms;
+        if (counts) counts[p] = h->phase[p].count;
+    }
+    return H4_OK;
+}
+
+const char *h4_phase_name(int phase) {
+    return (phase >= 0 && phase < PH_COUNT) ? kPhaseNames[phase] : "";
 }
 
 int h4_kernel_launches(h4_handle h, unsigned long long *count) {

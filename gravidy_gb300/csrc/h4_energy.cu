@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(EW * 32) k_energy_pairs(H4Dev d) {
             for (int q = 0; q < EI; q++) {
                 int j = ieff[q] + off;   // < 3n/2
                 if (j >= n) j -= n;
+                if (!range_ok(d, BS_ENERGY, j, j + 1ll, n)) continue;
                 const dbl4 rj = d.r[j];
                 const double dx = rj.x - xi[q], dy = rj.y - yi[q], dz = rj.z - zi[q];
                 const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));

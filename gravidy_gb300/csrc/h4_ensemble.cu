@@ -78,7 +78,8 @@ struct Dev {
     unsigned *queue;             // force work-queue head (warp items)
     unsigned *queue_b;           // force work-queue head (block items)
     unsigned *bar_count, *bar_gen;
-    unsigned *err;               // global error bits
+    unsigned *err;               // [2]: global error bits, first failing bounds-check site
+    size_t part_total;           // doubles in part
     unsigned *tune_ig, *tune_chunk;   // [NB_N * NB_A]
     unsigned *forced_nact;       // tuning probe: active count forced on every system (0 = off)
     unsigned long long *launches;     // persistent-kernel launches so far
@@ -86,6 +87,33 @@ struct Dev {
     double *epot_i, *energy;     // energy: per particle, per system (kin, pot)
     int mode;
 };
+
+// Bounds-checked build: [lo, hi) within [0, cap) (always true otherwise).
+__device__ __forceinline__ bool in_range(const Dev &d, unsigned code, long long lo, long long hi, long long cap) {
+    return range_ok(d.err, d.err + 1, code, lo, hi, cap);
+}
+
+// Bounds-checked build: a system's particle range and partial-force area.
+__device__ __forceinline__ bool system_ok(const Dev &d, const System &S) {
+    return in_range(d, BS_ENS_SYS, S.off, (long long)S.off + S.n, d.total) &&
+           in_range(d, BS_ENS_PART, (long long)S.part_off, (long long)(S.part_off + S.part_cap),
+                    (long long)d.part_total);
+}
+
+// Bounds-checked build: the ranges of one force item of system S -- its slice
+// of the active list ([k0, k0 + cnt) of nact <= n), its j range, its slice of
+// the system's partial-force area, and (lanes < cnt) the particle indices.
+__device__ bool item_ok(const Dev &d, const System &S, unsigned s, unsigned k0, unsigned cnt, int jb, int je,
+                        unsigned lane) {
+    bool ok = system_ok(d, S) && in_range(d, BS_ENS_ITEM, 0, S.nact, S.n) &&
+              in_range(d, BS_ENS_ITEM, k0, (long long)k0 + cnt, S.nact) && in_range(d, BS_ENS_ITEM, jb, je, S.n) &&
+              in_range(d, BS_ENS_PART, 6ll * S.nact * s, 6ll * S.nact * (s + 1), (long long)S.part_cap);
+    if (ok && lane < cnt) {
+        const unsigned i = d.move[S.off + k0 + lane];
+        ok = in_range(d, BS_MOVE, i, i + 1ll, S.n);
+    }
+    return ok;
+}
 
 // Grid-wide barrier of a cooperative launch, bounded in time.
 __device__ bool grid_sync(const Dev &d) {
@@ -165,6 +193,10 @@ __device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *re
     const unsigned forced = *d.forced_nact;
     unsigned nact = 0;
     double itime = 0.0;
+    if (!system_ok(d, S)) {   // bounds-checked build only
+        if (threadIdx.x == 0) { S.items = 0; S.bitems = 0; S.nact = 0; S.done = 1u; }
+        return;
+    }
     if (init || forced) {
         if (!init && S.done) {
             if (threadIdx.x == 0) { S.items = 0; S.bitems = 0; S.nact = 0; }
@@ -212,6 +244,7 @@ __device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *re
             }
             unsigned tot;
             unsigned pos = nact + block_scan_u(cnt, red, &tot);
+            if (cnt && !in_range(d, BS_SCATTER, pos, (long long)pos + cnt, n)) flags = 0;
 #pragma unroll
             for (int q = 0; q < 8; q++)
                 if (flags & (1u << q)) d.move[off + pos++] = (unsigned)(i0 + q);
@@ -325,6 +358,8 @@ __device__ void force_item(const Dev &d, const System &S, unsigned local, int la
     const unsigned *move = d.move + off;
     if (MODE == H4_FORCE_EXACT) {
         const unsigned k = g * 32 + lane;
+        const unsigned cnt = min(32u, nact - g * 32);
+        if (kBoundsCheck && !__all_sync(0xffffffffu, item_ok(d, S, s, g * 32, cnt, 0, S.n, (unsigned)lane))) return;
         if (k < nact) {
             double f[6];
             pair::exact_sum(d.pr + off, d.pv + off, S.n, move[k], S.e2, f);
@@ -335,6 +370,7 @@ __device__ void force_item(const Dev &d, const System &S, unsigned local, int la
     }
     const unsigned k0 = g * S.ig;
     const unsigned cnt = min(S.ig, nact - k0);
+    if (kBoundsCheck && !__all_sync(0xffffffffu, item_ok(d, S, s, k0, cnt, jb, je, (unsigned)lane))) return;
     if (MODE == H4_FORCE_FP64) {
         const dbl4 *pr = d.pr + off, *pv = d.pv + off;
         if (cnt == 4) {
@@ -381,6 +417,15 @@ __device__ void block_item(const Dev &d, const System &S, unsigned local, float4
     const int je = min(n, jb + (int)S.chunk);
     const unsigned k0 = g * BTI + threadIdx.x, k1 = k0 + THREADS;
     const unsigned *move = d.move + off;
+    if (kBoundsCheck) {   // block-uniform ranges, then this thread's two particle indices
+        const unsigned kb = g * BTI, cnt = min((unsigned)BTI, nact - kb);
+        if (!__syncthreads_and(item_ok(d, S, s, kb, cnt, jb, je, THREADS) &&
+                               in_range(d, BS_ENS_ITEM, (long long)off + jb, (long long)off + je, d.total)))
+            return;
+        if (!__syncthreads_and(in_range(d, BS_MOVE, move[k0 < nact ? k0 : nact - 1], move[k0 < nact ? k0 : nact - 1] + 1ll, n) &&
+                               in_range(d, BS_MOVE, move[k1 < nact ? k1 : nact - 1], move[k1 < nact ? k1 : nact - 1] + 1ll, n)))
+            return;
+    }
     const float4 *jf0 = d.jf0 + off, *jf1 = d.jf1 + off, *jf2 = d.jf2 + off;
     const IParticle a = load_i(jf0, jf1, jf2, move[k0 < nact ? k0 : nact - 1]);
     const IParticle b = load_i(jf0, jf1, jf2, move[k1 < nact ? k1 : nact - 1]);
@@ -433,18 +478,21 @@ __device__ void block_item(const Dev &d, const System &S, unsigned local, float4
 
 // ---- phase D (grid-wide): reduction, corrector and timestep of one active
 // particle (init: forces and the initial timestep) -----------------------------
-__device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k, bool init) {
-    const unsigned nact = S.nact, split = S.split;
+// Bounds-checked build: the ranges the reduction and corrector of active
+// particle k of system S touch.
+__device__ __forceinline__ bool correct_ok(const Dev &d, const System &S, unsigned k) {
+    if (!kBoundsCheck) return true;
+    if (!(system_ok(d, S) && in_range(d, BS_ENS_ITEM, k, k + 1ll, S.nact) &&
+          in_range(d, BS_ENS_PART, 0, 6ll * S.nact * S.split, (long long)S.part_cap)))
+        return false;
+    const unsigned i = d.move[S.off + k];
+    return in_range(d, BS_MOVE, i, i + 1ll, S.n);
+}
+
+// fn: the sum of the particle's partial forces (exact::sum_partials_*).
+__device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k, bool init, const double fn[6]) {
     const unsigned i = d.move[S.off + k];
     const size_t g = (size_t)S.off + i;
-    double fn[6];
-#pragma unroll
-    for (int q = 0; q < 6; q++) fn[q] = 0.0;
-    for (unsigned s = 0; s < split; s++) {
-        const double *p = d.part + S.part_off + (size_t)s * 6 * nact;
-#pragma unroll
-        for (int q = 0; q < 6; q++) fn[q] = exact::add(fn[q], p[(size_t)q * nact + k]);
-    }
     double *fp = d.f + 6 * g;
     if (init) {
 #pragma unroll
@@ -559,10 +607,26 @@ __global__ void __launch_bounds__(THREADS) k_ensemble(Dev d, int iters, int init
         }
         if (!grid_sync(d)) return;
         if (force_only) return;
-        // D: corrector of every active particle
+        // D: corrector of every active particle; the partial forces of
+        // systems with many j-chunks are summed by a warp per particle
+        // (lane 0 corrects), the others by a thread per particle
+        for (unsigned a = gtid >> 5; a < c_a; a += nthreads >> 5) {
+            const int c = find_seg(s_act, d.nsys, a);
+            System &S = d.sys[c];
+            const unsigned k = a - s_act[c];
+            if (!exact::warp_reduce(S.split) || !__all_sync(0xffffffffu, correct_ok(d, S, k))) continue;
+            double fn[6];
+            exact::sum_partials_warp(d.part + S.part_off, S.nact, k, S.split, lane, fn);
+            if (lane == 0) correct_one(d, S, k, init != 0, fn);
+        }
         for (unsigned a = gtid; a < c_a; a += nthreads) {
             const int c = find_seg(s_act, d.nsys, a);
-            correct_one(d, d.sys[c], a - s_act[c], init != 0);
+            System &S = d.sys[c];
+            const unsigned k = a - s_act[c];
+            if (exact::warp_reduce(S.split) || !correct_ok(d, S, k)) continue;
+            double fn[6];
+            exact::sum_partials_thread(d.part + S.part_off, S.nact, k, S.split, fn);
+            correct_one(d, S, k, init != 0, fn);
         }
         if (!grid_sync(d)) return;
         if (init) {
@@ -879,8 +943,9 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
 #define EA(p, cnt) if (e == cudaSuccess) e = dalloc(E, &p, cnt)
     EA(d.sys, nsys); EA(d.r, total); EA(d.v, total); EA(d.pr, total); EA(d.pv, total);
     EA(d.f, 6 * total); EA(d.old, 6 * total); EA(d.a2, 3 * total); EA(d.a3, 3 * total);
+    d.part_total = part_total;
     EA(d.t, total); EA(d.dt, total); EA(d.move, total); EA(d.part, part_total);
-    EA(d.queue, 1); EA(d.queue_b, 1); EA(d.bar_count, 1); EA(d.bar_gen, 1); EA(d.err, 1);
+    EA(d.queue, 1); EA(d.queue_b, 1); EA(d.bar_count, 1); EA(d.bar_gen, 1); EA(d.err, 2);
     EA(d.tune_ig, NB_N * NB_A); EA(d.tune_chunk, NB_N * NB_A); EA(d.forced_nact, 1); EA(d.launches, 1);
     EA(d.epot_i, total); EA(d.energy, 2 * nsys);
     if (mode == H4_FORCE_MIXED) { EA(d.jf0, total); EA(d.jf1, total); EA(d.jf2, total); EA(d.jd, 5 * total); }
@@ -907,7 +972,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     if (e == cudaSuccess) e = cudaMemsetAsync(d.queue_b, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.bar_count, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.bar_gen, 0, 4, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d.err, 0, 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.err, 0, 8, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.forced_nact, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.launches, 0, 8, s);
     // persistent grid: every block resident (cooperative launch)
@@ -1023,6 +1088,11 @@ int h4_ens_advance(h4_ens_handle E, const double *t_end, double stats[4]) {
         stats[1] = (double)ps;
         stats[2] = (double)inter;
         stats[3] = (double)nl;
+    }
+    if (err & H4_ERRBIT_BOUNDS) {
+        unsigned w[2] = {0, 0};
+        ENS_TRY(cudaMemcpy(w, E->d.err, 8, cudaMemcpyDeviceToHost), "error word");
+        return efail(H4_ERR_STATE, "h4_ens_advance: bounds check failed at site " + std::to_string(w[1]));
     }
     if (err & H4_ERRBIT_TIMEOUT) return efail(H4_ERR_CUDA, "h4_ens_advance: a grid barrier timed out");
     if (err & H4_ERRBIT_NONFINITE) return efail(H4_ERR_NONFINITE, "h4_ens_advance: non-finite state in a system");

@@ -184,5 +184,46 @@ __device__ __forceinline__ double init_dt(const double *f, double eta, double dt
     return tmp;
 }
 
+// ---- j-split partial forces -------------------------------------------------
+// The force kernels leave, for active particle k and j-chunk s, the partial sum
+// of component c at part[(s * 6 + c) * nact + k].  Their sum is formed in one
+// of two fixed orders, chosen by the chunk count S alone:
+//  * a thread per particle adds the chunks in chunk order;
+//  * with many chunks (S >= WARP_REDUCE_MIN_S, small active sets) a warp per
+//    particle does it: lane l adds chunks l, l + 32, ... in order, then a
+//    fixed shuffle tree.  A chain of S dependent FP64 additions per thread
+//    would otherwise, at GB300's FP64 rate, take longer than the force sum
+//    of a small active set.
+constexpr unsigned WARP_REDUCE_MIN_S = 32;
+
+__device__ __forceinline__ bool warp_reduce(unsigned S) { return S >= WARP_REDUCE_MIN_S; }
+
+__device__ __forceinline__ void sum_partials_thread(const double *part, unsigned nact, unsigned k, unsigned S,
+                                                    double out[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; c++) out[c] = 0.0;
+    for (unsigned s = 0; s < S; s++) {
+        const double *p = part + (size_t)s * 6 * nact;
+#pragma unroll
+        for (int c = 0; c < 6; c++) out[c] = add(out[c], p[(size_t)c * nact + k]);
+    }
+}
+
+// All 32 lanes call it with the same k; the sum is in lane 0.
+__device__ __forceinline__ void sum_partials_warp(const double *part, unsigned nact, unsigned k, unsigned S, int lane,
+                                                  double out[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; c++) out[c] = 0.0;
+    for (unsigned s = lane; s < S; s += 32) {
+        const double *p = part + (size_t)s * 6 * nact;
+#pragma unroll
+        for (int c = 0; c < 6; c++) out[c] = add(out[c], p[(size_t)c * nact + k]);
+    }
+#pragma unroll
+    for (int c = 0; c < 6; c++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) out[c] = add(out[c], __shfl_down_sync(0xffffffffu, out[c], o));
+}
+
 }  // namespace exact
 }  // namespace h4

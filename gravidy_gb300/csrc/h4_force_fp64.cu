@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_force_fp64(H4Dev d) {
         const unsigned k0 = g * IG;
         const unsigned cnt = min((unsigned)IG, nact - k0);
         double *part_s = d.part + (size_t)s * 6 * nact;
+        if (kBoundsCheck && !pair::warp_item_ok(d, nact, k0, cnt, j_begin, j_end, s, lane, BS_FP64_J)) continue;
         if (cnt == (unsigned)IG) {
             pair::fp64_warp_item<IG>(d.pr, d.pv, d.move, nact, k0, j_begin, j_end, d.e2, part_s, lane);
         } else {
@@ -100,6 +101,9 @@ __global__ void __launch_bounds__(128) k_force_exact(H4Dev d) {
     const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
     if (blockIdx.x == 0 && threadIdx.x == 0) d.ctrl->force_split = 1;
     if (k >= nact) return;
+    if (!range_ok(d, BS_NACT, 0, nact, d.n) || !range_ok(d, BS_PART, 0, 6ll * nact, (long long)d.part_cap) ||
+        !range_ok(d, BS_MOVE, d.move[k], d.move[k] + 1ll, d.n))
+        return;
     double f[6];
     pair::exact_sum(d.pr, d.pv, d.n, d.move[k], d.e2, f);
 #pragma unroll

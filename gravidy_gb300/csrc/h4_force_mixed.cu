@@ -108,6 +108,20 @@ __device__ __forceinline__ MixedSplit tiled_split(const H4Dev &d, unsigned nact,
     return s;
 }
 
+// Bounds-checked build: the ranges of one tiled item -- whole tiles of the
+// padded j arrays, its slice of the partial-force area.  Block-uniform.
+__device__ __forceinline__ bool tiled_item_ok(const H4Dev &d, unsigned nact, unsigned s, int j_begin, int j_end) {
+    return range_ok(d, BS_NACT, 0, nact, d.n) && range_ok(d, BS_MIXED_J, j_begin, j_end, d.n_pad) &&
+           range_ok(d, BS_MIXED_J, 0, (j_end - j_begin) % JT, 1) &&
+           range_ok(d, BS_PART, 6ll * nact * s, 6ll * nact * (s + 1), (long long)d.part_cap);
+}
+
+// Bounds-checked build: a particle index of the active list (skipped: 0).
+__device__ __forceinline__ unsigned checked_move(const H4Dev &d, unsigned k) {
+    const unsigned i = d.move[k];
+    return range_ok(d, BS_MOVE, i, i + 1ll, d.n) ? i : 0u;
+}
+
 template <bool MASK_SELF>
 __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled(H4Dev d, unsigned threshold) {
     __shared__ __align__(128) float4 sj[2][3][JT];
@@ -140,6 +154,7 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled(H4Dev d, unsigned t
         const int j_begin = (int)s * sp.chunk;
         const int j_end = min(d.n_pad, j_begin + sp.chunk);
         const int ntiles = (j_end - j_begin) / JT;
+        if (kBoundsCheck && !tiled_item_ok(d, nact, s, j_begin, j_end)) continue;
 
         IParticle ip[IPT];
         unsigned idx[IPT];
@@ -147,7 +162,7 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled(H4Dev d, unsigned t
 #pragma unroll
         for (int q = 0; q < IPT; q++) {
             const unsigned k = g * TI + tid + q * MT;
-            idx[q] = d.move[k < nact ? k : nact - 1];
+            idx[q] = checked_move(d, k < nact ? k : nact - 1);
             ip[q] = load_i(d, idx[q]);
 #pragma unroll
             for (int c = 0; c < 6; c++) { S[q][c] = 0.f; C[q][c] = 0.f; }
@@ -274,14 +289,15 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled_x2(H4Dev d, unsigne
         const int j_begin = (int)s * sp.chunk;
         const int j_end = min(d.n_pad, j_begin + sp.chunk);
         const int ntiles = (j_end - j_begin) / JT;
+        if (kBoundsCheck && !tiled_item_ok(d, nact, s, j_begin, j_end)) continue;
 
         IPair ip[NPK];
         f2 S[NPK][6], Cc[NPK][6];
 #pragma unroll
         for (int q = 0; q < NPK; q++) {
             const unsigned k0 = g * TI + tid + (2 * q) * MT, k1 = k0 + MT;
-            const IParticle a = load_i(d, d.move[k0 < nact ? k0 : nact - 1]);
-            const IParticle b = load_i(d, d.move[k1 < nact ? k1 : nact - 1]);
+            const IParticle a = load_i(d, checked_move(d, k0 < nact ? k0 : nact - 1));
+            const IParticle b = load_i(d, checked_move(d, k1 < nact ? k1 : nact - 1));
             ip[q].xh = pk2(a.xh, b.xh); ip[q].yh = pk2(a.yh, b.yh); ip[q].zh = pk2(a.zh, b.zh);
             ip[q].xl = pk2(a.xl, b.xl); ip[q].yl = pk2(a.yl, b.yl); ip[q].zl = pk2(a.zl, b.zl);
             ip[q].vx = pk2(a.vx, b.vx); ip[q].vy = pk2(a.vy, b.vy); ip[q].vz = pk2(a.vz, b.vz);
@@ -398,6 +414,7 @@ __global__ void __launch_bounds__(WARPS_W * 32) k_force_mixed_warp(H4Dev d, unsi
         const unsigned k0 = g * IGW;
         const unsigned cnt = min((unsigned)IGW, nact - k0);
         double *part_s = d.part + (size_t)s * 6 * nact;
+        if (kBoundsCheck && !pair::warp_item_ok(d, nact, k0, cnt, j_begin, j_end, s, lane, BS_MIXED_WJ)) continue;
         if (cnt == 4) {
             pair::mixed_warp_item<4, MASK_SELF>(d.jf0, d.jf1, d.jf2, d.move, nact, k0, j_begin, j_end, e2, part_s, lane);
         } else {

@@ -37,7 +37,7 @@ struct H4Ctrl {
     unsigned long long max_steps;  // hard bound on steps of one advance call
     unsigned long long nact_hist[32]; // block steps by floor(log2(nact)), since creation
     int running;                   // 1 while the device loop continues
-    int pad_;
+    unsigned int bounds_site;      // first failing check of the bounds-checked build (0 = none)
 };
 
 enum : unsigned int {
@@ -45,7 +45,51 @@ enum : unsigned int {
     H4_ERRBIT_SPLIT = 2u,          // partial-force scratch too small
     H4_ERRBIT_STEPCAP = 4u,        // device loop reached its step bound
     H4_ERRBIT_TIMEOUT = 8u,        // a bounded wait (mbarrier) gave up
+    H4_ERRBIT_BOUNDS = 16u,        // an index check of the bounds-checked build failed
 };
+
+// ---- bounds-checked build -----------------------------------------------------
+// Compiled with -DH4_BOUNDS_CHECK, every kernel checks the index ranges it is
+// about to touch (the active list and the particle indices in it, the j range
+// and the partial-force area of a work item, a system's particle range in an
+// ensemble) before touching them.  A violation sets H4_ERRBIT_BOUNDS, keeps
+// the first failing site, and the access is skipped instead of made; the
+// host reports it as an error.  This stands in for a memory checker.  In the
+// normal build kBoundsCheck is false and every check folds away.
+#ifdef H4_BOUNDS_CHECK
+constexpr bool kBoundsCheck = true;
+#else
+constexpr bool kBoundsCheck = false;
+#endif
+
+// Sites of the checks (the value kept in bounds_site).
+enum : unsigned int {
+    BS_NACT = 1,          // active count within the particle count
+    BS_SCATTER = 2,       // active-list writes of the ordered compaction
+    BS_MOVE = 3,          // a particle index read from the active list
+    BS_PART = 4,          // partial-force area of a work item or of the reduction
+    BS_FP64_J = 5,        // j range of an FP64 warp item
+    BS_FP64_K = 6,        // active-list range of an FP64 warp item
+    BS_MIXED_J = 7,       // j range (tiles) of a mixed tiled item
+    BS_MIXED_K = 8,       // active-list range of a mixed item
+    BS_MIXED_WJ = 9,      // j range of a mixed warp item
+    BS_ENERGY = 10,       // pair range of the energy kernel
+    BS_ENS_SYS = 11,      // an ensemble system's particle range
+    BS_ENS_ITEM = 12,     // an ensemble force item's ranges
+    BS_ENS_PART = 13,     // an ensemble system's partial-force area
+    BS_NOALLOC = 14,      // ranges of the allocation-free force sum
+    BS_DIAG = 15,         // diagnostics kernels
+};
+
+// [lo, hi) within [0, cap).  Always true in the normal build.
+__device__ __forceinline__ bool range_ok(unsigned *err, unsigned *site, unsigned code, long long lo,
+                                         long long hi, long long cap) {
+    if (!kBoundsCheck) return true;
+    if (lo >= 0 && lo <= hi && hi <= cap) return true;
+    atomicOr(err, (unsigned)H4_ERRBIT_BOUNDS);
+    atomicCAS(site, 0u, code);
+    return false;
+}
 
 // Device clock in ns (%globaltimer).
 __device__ __forceinline__ unsigned long long device_ns() {
@@ -91,6 +135,11 @@ struct H4Dev {
     double *energy_out;     // [2] kinetic, potential
     H4Ctrl *ctrl;
 };
+
+__device__ __forceinline__ bool range_ok(const H4Dev &d, unsigned code, long long lo, long long hi,
+                                         long long cap) {
+    return range_ok(&d.ctrl->err, &d.ctrl->bounds_site, code, lo, hi, cap);
+}
 
 constexpr int FLAG_THREADS = 256;
 constexpr int FLAG_ITEMS = 8;                       // elements per thread

@@ -114,6 +114,13 @@ extern "C" int h4_forces_noalloc(unsigned int n, double e2, const h4_double4 *d_
     launch_reduce_to(d, (double *)d_out, s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return noalloc_fail(H4_ERR_CUDA, "kernel launch", e);
+    if (kBoundsCheck) {   // bounds-checked build: wait and read the error word
+        H4Ctrl c;
+        e = cudaStreamSynchronize(s);
+        if (e == cudaSuccess) e = cudaMemcpy(&c, nd->ctrl, sizeof(c), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return noalloc_fail(H4_ERR_CUDA, "control block", e);
+        if (c.err & H4_ERRBIT_BOUNDS) return noalloc_fail(H4_ERR_STATE, "bounds check failed");
+    }
     return H4_OK;
 }
 

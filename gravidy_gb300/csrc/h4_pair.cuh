@@ -54,6 +54,85 @@ __device__ __forceinline__ void pair_fp64(double xi, double yi, double zi, doubl
     acc[5] = fma(A, fma(eta, dz, dvz), acc[5]);
 }
 
+// ---- lane sums of a warp item ---------------------------------------------------
+// A warp item ends with 6 * NI sums per lane to be added over the 32 lanes.
+// A shuffle tree per value costs 5 additions per value; a butterfly
+// reduce-scatter costs 31 in all for 32 values: at offset o each lane keeps
+// half of its values, adds the partner's copies of them, and sends the other
+// half.  With V = 2^L values, lane t ends holding the total of value
+// t >> (5 - L) (the lanes that share it hold the same total), in a fixed
+// order.  On GB300 this matters: the FP64 pipe runs a warp-wide addition at
+// 1/64 of the FP32 rate, and the per-value trees cost as much as the pair
+// arithmetic of a short j-chunk.
+
+// Smallest power of two >= x (x <= 32).
+__host__ __device__ constexpr int pow2_ceil(int x) { return x <= 1 ? 1 : 2 * pow2_ceil((x + 1) / 2); }
+__host__ __device__ constexpr int log2_exact(int x) { return x <= 1 ? 0 : 1 + log2_exact(x / 2); }
+
+template <int V, int O>
+__device__ __forceinline__ void rs_sum_f64(double *v, int lane) {
+    if constexpr (O > 0) {
+        if constexpr (V > 1) {
+            const bool upper = (lane & O) != 0;
+#pragma unroll
+            for (int k = 0; k < V / 2; k++) {
+                const double send = upper ? v[k] : v[k + V / 2];
+                const double keep = upper ? v[k + V / 2] : v[k];
+                v[k] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+            }
+            rs_sum_f64<V / 2, O / 2>(v, lane);
+        } else {
+            v[0] = v[0] + __shfl_xor_sync(0xffffffffu, v[0], O);
+            rs_sum_f64<1, O / 2>(v, lane);
+        }
+    }
+}
+
+// Error-free sum (Knuth's TwoSum): s + e == a + b exactly, for any order of
+// magnitudes.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+
+// (h + l) += (h2 + l2) in double-single arithmetic (a float pair), renormalised.
+__device__ __forceinline__ void ds_add(float &h, float &l, float h2, float l2) {
+    float s, e;
+    two_sum(h, h2, s, e);
+    e = e + (l + l2);
+    h = s + e;
+    l = e - (h - s);
+}
+
+template <int V, int O>
+__device__ __forceinline__ void rs_sum_ds(float *h, float *l, int lane) {
+    if constexpr (O > 0) {
+        if constexpr (V > 1) {
+            const bool upper = (lane & O) != 0;
+#pragma unroll
+            for (int k = 0; k < V / 2; k++) {
+                const float sh = upper ? h[k] : h[k + V / 2], sl = upper ? l[k] : l[k + V / 2];
+                float kh = upper ? h[k + V / 2] : h[k], kl = upper ? l[k + V / 2] : l[k];
+                ds_add(kh, kl, __shfl_xor_sync(0xffffffffu, sh, O), __shfl_xor_sync(0xffffffffu, sl, O));
+                h[k] = kh;
+                l[k] = kl;
+            }
+            rs_sum_ds<V / 2, O / 2>(h, l, lane);
+        } else {
+            ds_add(h[0], l[0], __shfl_xor_sync(0xffffffffu, h[0], O), __shfl_xor_sync(0xffffffffu, l[0], O));
+            rs_sum_ds<1, O / 2>(h, l, lane);
+        }
+    }
+}
+
+// Value index held by `lane` after a reduce-scatter of V values, and whether
+// the lane is the first of those holding it.
+template <int V>
+__device__ __forceinline__ int rs_index(int lane) { return lane >> (5 - log2_exact(V)); }
+template <int V>
+__device__ __forceinline__ bool rs_first(int lane) { return (lane & ((32 / V) - 1)) == 0; }
+
 template <int NI>
 __device__ __forceinline__ void fp64_warp_item(const dbl4 *__restrict__ pr, const dbl4 *__restrict__ pv,
                                                const unsigned *__restrict__ move, unsigned nact, unsigned k0,
@@ -77,16 +156,29 @@ __device__ __forceinline__ void fp64_warp_item(const dbl4 *__restrict__ pr, cons
         for (int q = 0; q < NI; q++)
             pair_fp64(xi[q], yi[q], zi[q], vxi[q], vyi[q], vzi[q], pj, vj, e2, (unsigned)j == idx[q], acc[q]);
     }
+    // value c * NI + q = component c of particle q; zero padding to V
+    constexpr int V = pow2_ceil(6 * NI);
+    double val[V];
 #pragma unroll
-    for (int q = 0; q < NI; q++) {
-#pragma unroll
-        for (int c = 0; c < 6; c++) {
-            double a = acc[q][c];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-            if (lane == 0) part_s[(size_t)c * nact + k0 + q] = a;
-        }
+    for (int x = 0; x < V; x++) val[x] = x < 6 * NI ? acc[x % NI][x / NI] : 0.0;
+    rs_sum_f64<V, 16>(val, lane);
+    const int x = rs_index<V>(lane);
+    if (rs_first<V>(lane) && x < 6 * NI) part_s[(size_t)(x / NI) * nact + k0 + (x % NI)] = val[0];
+}
+
+// Bounds-checked build: every range one single-system warp item touches --
+// its slice of the active list, the particle indices in it, its j range and
+// its slice of the partial-force area ([S][6][nact]).  Warp-uniform result.
+__device__ __forceinline__ bool warp_item_ok(const H4Dev &d, unsigned nact, unsigned k0, unsigned cnt, int j_begin,
+                                             int j_end, unsigned s, int lane, unsigned site_j) {
+    bool ok = range_ok(d, BS_NACT, 0, nact, d.n) && range_ok(d, BS_FP64_K, k0, (long long)k0 + cnt, nact) &&
+              range_ok(d, site_j, j_begin, j_end, d.n) &&
+              range_ok(d, BS_PART, 6ll * nact * s, 6ll * nact * (s + 1), (long long)d.part_cap);
+    if (ok && (unsigned)lane < cnt) {
+        const unsigned i = d.move[k0 + lane];
+        ok = range_ok(d, BS_MOVE, i, i + 1ll, d.n);
     }
+    return __all_sync(0xffffffffu, ok);
 }
 
 // Bit-identical restatement of the reference's per-particle sum (one thread,
@@ -206,16 +298,19 @@ __device__ __forceinline__ void mixed_warp_item(const float4 *__restrict__ jf0, 
 #pragma unroll
             for (int c = 0; c < 6; c++) kahan_add(S[q][c], C[q][c], part[q][c]);
     }
+    // Kahan pairs (value S - C) summed over the lanes in double-single FP32;
+    // value c * NI + q = component c of particle q; zero padding to V
+    constexpr int V = pow2_ceil(6 * NI);
+    float h[V], l[V];
 #pragma unroll
-    for (int q = 0; q < NI; q++) {
-#pragma unroll
-        for (int c = 0; c < 6; c++) {
-            double a = (double)S[q][c] - (double)C[q][c];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-            if (lane == 0) part_s[(size_t)c * nact + k0 + q] = a;
-        }
+    for (int x = 0; x < V; x++) {
+        h[x] = x < 6 * NI ? S[x % NI][x / NI] : 0.f;
+        l[x] = x < 6 * NI ? -C[x % NI][x / NI] : 0.f;
     }
+    rs_sum_ds<V, 16>(h, l, lane);
+    const int x = rs_index<V>(lane);
+    if (rs_first<V>(lane) && x < 6 * NI)
+        part_s[(size_t)(x / NI) * nact + k0 + (x % NI)] = (double)h[0] + (double)l[0];
 }
 
 // ---- packed f32x2 arithmetic (sm_100+) ---------------------------------------

@@ -121,6 +121,7 @@ k_flag_scatter(H4Dev d, int nblocks) {
         if (i < d.n && is_active(itime, d.t[i], d.dt[i])) { flags |= 1u << q; c++; }
     }
     unsigned off = before + block_exclusive_scan(c);
+    if (c && !range_ok(d, BS_SCATTER, off, (long long)off + c, d.n)) flags = 0;
 #pragma unroll
     for (int q = 0; q < FLAG_ITEMS; q++)
         if (flags & (1u << q)) d.move[off++] = (unsigned)(base + q);
@@ -139,8 +140,10 @@ k_flag_scatter(H4Dev d, int nblocks) {
 // ---- Hermite4::save_old_acc_jrk (Hermite4.cpp:145-153) ----------------------
 __global__ void k_save_old(H4Dev d) {
     const unsigned nact = d.ctrl->nact;
+    if (!range_ok(d, BS_NACT, 0, nact, d.n)) return;
     for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nact; k += gridDim.x * blockDim.x) {
         const unsigned i = d.move[k];
+        if (!range_ok(d, BS_MOVE, i, i + 1ll, d.n)) continue;
 #pragma unroll
         for (int c = 0; c < 6; c++) d.old[6 * (size_t)i + c] = d.f[6 * (size_t)i + c];
     }
@@ -191,24 +194,41 @@ __global__ void k_identity_move(H4Dev d) {
     }
 }
 
-// Sum of the j-split partial forces of active particle k, in chunk order.
-__device__ __forceinline__ void reduce_partials(const H4Dev &d, unsigned k, unsigned nact,
-                                                unsigned S, double out[6]) {
-#pragma unroll
-    for (int c = 0; c < 6; c++) out[c] = 0.0;
-    for (unsigned s = 0; s < S; s++) {
-        const double *p = d.part + (size_t)s * 6 * nact;
-#pragma unroll
-        for (int c = 0; c < 6; c++) out[c] = add(out[c], p[(size_t)c * nact + k]);
+// Calls body(k, f) for every active particle k with the sum f of its j-split
+// partial forces, over the whole grid: a thread per particle, or a warp per
+// particle with body called by lane 0 (exact::warp_reduce(S)).  blockDim is a
+// multiple of 32.
+template <class Body>
+__device__ __forceinline__ void for_each_reduced(const H4Dev &d, unsigned nact, unsigned S, Body body) {
+    const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    if (exact::warp_reduce(S)) {
+        const int lane = threadIdx.x & 31;
+        for (unsigned k = gt >> 5; k < nact; k += nt >> 5) {
+            double f[6];
+            exact::sum_partials_warp(d.part, nact, k, S, lane, f);
+            if (lane == 0) body(k, f);
+        }
+    } else {
+        for (unsigned k = gt; k < nact; k += nt) {
+            double f[6];
+            exact::sum_partials_thread(d.part, nact, k, S, f);
+            body(k, f);
+        }
     }
+}
+
+// The active list and the partial-force area the reduction reads (checked
+// build only).
+__device__ __forceinline__ bool reduce_ranges_ok(const H4Dev &d, unsigned nact, unsigned S) {
+    return range_ok(d, BS_NACT, 0, nact, d.n) && range_ok(d, BS_PART, 0, 6ll * nact * S, (long long)d.part_cap);
 }
 
 __global__ void k_reduce_forces(H4Dev d, int save_old) {
     const unsigned nact = d.ctrl->nact, S = d.ctrl->force_split;
-    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nact; k += gridDim.x * blockDim.x) {
+    if (!reduce_ranges_ok(d, nact, S)) return;
+    for_each_reduced(d, nact, S, [&](unsigned k, const double *fn) {
         const unsigned i = d.move[k];
-        double fn[6];
-        reduce_partials(d, k, nact, S, fn);
+        if (!range_ok(d, BS_MOVE, i, i + 1ll, d.n)) return;
         double *f = d.f + 6 * (size_t)i;
         if (save_old) {
 #pragma unroll
@@ -216,38 +236,50 @@ __global__ void k_reduce_forces(H4Dev d, int save_old) {
         }
 #pragma unroll
         for (int c = 0; c < 6; c++) f[c] = fn[c];
-    }
+    });
 }
 
 // ---- Hermite4CPU::correction_pos_vel (Hermite4CPU.cpp:370-411) --------------
 // with NbodyUtils::get_timestep_normal (NbodyUtils.cpp:337-365).
+// fn: the new forces when the reduction is fused here, else null (the forces
+// were reduced into d.f and the old ones saved by k_reduce_forces).
+__device__ __forceinline__ void correct_particle(const H4Dev &d, unsigned k, double itime, const double *fn) {
+    const unsigned i = d.move[k];
+    if (!range_ok(d, BS_MOVE, i, i + 1ll, d.n)) return;
+    double *fp = d.f + 6 * (size_t)i;
+    double *op = d.old + 6 * (size_t)i;
+    double f[6], o[6];
+    if (fn) {
+#pragma unroll
+        for (int c = 0; c < 6; c++) { f[c] = fn[c]; o[c] = fp[c]; op[c] = o[c]; fp[c] = f[c]; }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 6; c++) { f[c] = fp[c]; o[c] = op[c]; }
+    }
+    dbl4 r = d.r[i], v = d.v[i];
+    double a2[3], a3[3], ndt;
+    const bool ok = exact::correct(itime, d.eta, d.dt_min, d.dt_max, f, o, d.pr[i], d.pv[i], d.dt[i], r, v,
+                                   a2, a3, ndt);
+    d.r[i] = r;
+    d.v[i] = v;
+#pragma unroll
+    for (int c = 0; c < 3; c++) { d.a2[3 * (size_t)i + c] = a2[c]; d.a3[3 * (size_t)i + c] = a3[c]; }
+    d.t[i] = itime;
+    d.dt[i] = ndt;
+    if (!ok) atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_NONFINITE);
+}
+
 __global__ void __launch_bounds__(128) k_correct(H4Dev d, int host_itime, double itime_in, int fused_reduce) {
     const unsigned nact = d.ctrl->nact;
     const double itime = host_itime ? itime_in : d.ctrl->itime;
-    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nact; k += gridDim.x * blockDim.x) {
-        const unsigned i = d.move[k];
-        double *fp = d.f + 6 * (size_t)i;
-        double *op = d.old + 6 * (size_t)i;
-        double f[6], o[6];
-        if (fused_reduce) {
-            reduce_partials(d, k, nact, d.ctrl->force_split, f);
-#pragma unroll
-            for (int c = 0; c < 6; c++) { o[c] = fp[c]; op[c] = o[c]; fp[c] = f[c]; }
-        } else {
-#pragma unroll
-            for (int c = 0; c < 6; c++) { f[c] = fp[c]; o[c] = op[c]; }
-        }
-        dbl4 r = d.r[i], v = d.v[i];
-        double a2[3], a3[3], ndt;
-        const bool ok = exact::correct(itime, d.eta, d.dt_min, d.dt_max, f, o, d.pr[i], d.pv[i], d.dt[i], r, v,
-                                       a2, a3, ndt);
-        d.r[i] = r;
-        d.v[i] = v;
-#pragma unroll
-        for (int c = 0; c < 3; c++) { d.a2[3 * (size_t)i + c] = a2[c]; d.a3[3 * (size_t)i + c] = a3[c]; }
-        d.t[i] = itime;
-        d.dt[i] = ndt;
-        if (!ok) atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_NONFINITE);
+    if (fused_reduce) {
+        const unsigned S = d.ctrl->force_split;
+        if (!reduce_ranges_ok(d, nact, S)) return;
+        for_each_reduced(d, nact, S, [&](unsigned k, const double *fn) { correct_particle(d, k, itime, fn); });
+    } else {
+        if (!reduce_ranges_ok(d, nact, 0u)) return;
+        for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nact; k += gridDim.x * blockDim.x)
+            correct_particle(d, k, itime, nullptr);
     }
 }
 
@@ -293,12 +325,11 @@ __global__ void k_set_atime(H4Dev d, double atime) { d.ctrl->atime_bits = double
 // Fixed-order sum of the partial forces into out[6k + c] (Forces layout).
 __global__ void k_reduce_to(H4Dev d, double *out) {
     const unsigned nact = d.ctrl->nact, S = d.ctrl->force_split;
-    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nact; k += gridDim.x * blockDim.x) {
-        double fn[6];
-        reduce_partials(d, k, nact, S, fn);
+    if (!reduce_ranges_ok(d, nact, S)) return;
+    for_each_reduced(d, nact, S, [&](unsigned k, const double *fn) {
 #pragma unroll
         for (int c = 0; c < 6; c++) out[6 * (size_t)k + c] = fn[c];
-    }
+    });
 }
 
 // ---- per-step bookkeeping of the device-resident loop ------------------------

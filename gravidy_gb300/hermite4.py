@@ -289,6 +289,13 @@ class Hermite4GPU:
         _lib.check(self.L.h4_last_timings(self.h, C.byref(f), C.byref(a)))
         return f.value, a.value
 
+    def phase_times(self) -> dict:
+        """{phase: (device ms, calls)} with the reference's Gtime phase names."""
+        ms = np.zeros(8)
+        cnt = np.zeros(8, dtype=np.uint64)
+        _lib.check(self.L.h4_phase_times(self.h, ms.ctypes.data, cnt.ctypes.data))
+        return {self.L.h4_phase_name(k).decode(): (float(ms[k]), int(cnt[k])) for k in range(8)}
+
     def nact_histogram(self) -> np.ndarray:
         out = np.zeros(32, dtype=np.uint64)
         _lib.check(self.L.h4_nact_histogram(self.h, out.ctypes.data))

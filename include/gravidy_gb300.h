@@ -62,6 +62,13 @@ typedef struct h4_system_s *h4_handle;
 const char *h4_last_error(void);
 const char *h4_status_string(int status);
 int h4_abi_version(void);
+/* Build variant of the loaded library (no reference counterpart): bit
+ * H4_BUILD_BOUNDS_CHECK is set in the bounds-checked build, whose kernels
+ * check every index range before touching it and report a violation as
+ * H4_ERR_STATE ("bounds check failed at site N") instead of accessing memory
+ * out of bounds. */
+#define H4_BUILD_BOUNDS_CHECK 1
+int h4_build_flags(void);
 
 /* Creation.  Replaces Hermite4GPU::Hermite4GPU + alloc_arrays_device
  * (Hermite4GPU.cu:40-165) and Hermite4::init_data (Hermite4.cpp:194-240).
@@ -87,7 +94,7 @@ int h4_set_dt_limits(h4_handle h, double dt_min, double dt_max);
 int h4_set_force_mode(h4_handle h, int mode);
 /* H4_FORCE_MIXED: active-set size from which the shared-memory tiled kernel
  * (lanes over active particles) is used instead of warp items (lanes over j).
- * Default 64 for N >= 32768, else 256 (measured crossover on GB300). */
+ * Default 384 for N >= 65536, else 768 (measured crossover on GB300). */
 int h4_set_mixed_threshold(h4_handle h, unsigned int nact_threshold);
 
 /* Hermite4GPU::init_acc_jrk (Hermite4GPU.cu:333-375): acc and jerk of all
@@ -269,6 +276,14 @@ int h4_last_timings(h4_handle h, float *force_ms, float *advance_ms);
 /* Block steps run by h4_advance since creation, by active-set size:
  * counts[k] = steps with 2^k <= nact < 2^(k+1). */
 int h4_nact_histogram(h4_handle h, unsigned long long counts[32]);
+/* Device time per phase since creation, CUDA events on the handle's stream,
+ * with the phase names of the reference's Gtime (common.hpp:287-310):
+ * 0 prediction, 1 update (force sum + reduction), 2 grav (force kernel
+ * alone), 3 correction, 4 active_set, 5 next_time, 6 energy, 7 advance
+ * (device-resident loop; its inner phases are not split).  counts = calls. */
+#define H4_PHASES 8
+int h4_phase_times(h4_handle h, double ms[H4_PHASES], unsigned long long counts[H4_PHASES]);
+const char *h4_phase_name(int phase);
 /* Kernels launched by this handle since creation. */
 int h4_kernel_launches(h4_handle h, unsigned long long *count);
 

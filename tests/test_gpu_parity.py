@@ -192,3 +192,31 @@ def test_advance_graph_equals_host_driven_steps():
         sa, sb = a.download(), b.download()
         for k in ("r", "v", "f", "t", "dt"):
             assert np.array_equal(sa[k], sb[k]), k
+
+
+@pytest.mark.gpu
+def test_phase_timers_count_host_driven_calls():
+    """Per-phase device timers (the reference's Gtime phases, common.hpp:287-310)."""
+    ns = plummer_system(2048, seed=5)
+    with Hermite4GPU(ns) as g:
+        g.init_acc_jrk()
+        atime = g.init_dt(1.0e10, float(orc.ETA_S), 0.0)
+        steps = 6
+        for _ in range(steps):
+            itime = atime
+            nact = g.find_particles_to_move(itime)
+            g.save_old_acc_jrk(nact)
+            g.predicted_pos_vel(itime)
+            g.update_acc_jrk(nact)
+            g.correction_pos_vel(itime, nact)
+            atime = g.next_integration_time()
+        g.get_energy_gpu()
+        g.advance(atime + 2.0 ** -8, 1e30, atime)
+        ph = g.phase_times()
+    assert list(ph) == ["prediction", "update", "grav", "correction", "active_set",
+                        "next_time", "energy", "advance"]
+    for k in ("prediction", "update", "grav", "correction", "active_set", "next_time"):
+        assert ph[k][1] == steps, k
+        assert ph[k][0] > 0.0, k
+    assert ph["energy"][1] == 1 and ph["advance"][1] == 1
+    assert ph["grav"][0] <= ph["update"][0]
