@@ -73,6 +73,7 @@ SIGNATURES = {
     "h4_ens_system_stats": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "h4_ens_tune_force": (_i, [_vp, _u, _u, _u, C.POINTER(_f)]),
     "h4_ens_timings": (_i, [_vp, C.POINTER(_f), C.POINTER(C.c_ulonglong)]),
+    "h4_ens_phase_times": (_i, [_vp, _vp]),
     "h4_forces_noalloc_error": (C.c_char_p, []),
 }
 

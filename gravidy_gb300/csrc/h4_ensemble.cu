@@ -41,6 +41,10 @@
 namespace h4 {
 namespace ens {
 
+// Resident blocks per SM the register allocation must allow (build knob).
+#ifndef H4_ENS_MIN_BLOCKS
+#define H4_ENS_MIN_BLOCKS 1
+#endif
 constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
 constexpr int NB_N = H4_ENS_TUNE_NB_N;
@@ -83,6 +87,7 @@ struct Dev {
     unsigned *tune_ig, *tune_chunk;   // [NB_N * NB_A]
     unsigned *forced_nact;       // tuning probe: active count forced on every system (0 = off)
     unsigned long long *launches;     // persistent-kernel launches so far
+    unsigned long long *phase_ns;     // [4] device time of phases A, B, C, D since creation
     unsigned long long max_launches;
     double *epot_i, *energy;     // energy: per particle, per system (kin, pot)
     int mode;
@@ -521,8 +526,19 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
     }
 }
 
+// Phase timer: block 0 reads %globaltimer after every grid barrier and adds
+// the time since the previous one to its phase.  A barrier ends when the
+// last block reaches it, so this is the phase's duration on the whole GPU.
+__device__ __forceinline__ void phase_mark(const Dev &d, int phase, unsigned long long &t_prev) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const unsigned long long t = device_ns();
+        d.phase_ns[phase] += t - t_prev;
+        t_prev = t;
+    }
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(THREADS) k_ensemble(Dev d, int iters, int init, int force_only) {
+__global__ void __launch_bounds__(THREADS, H4_ENS_MIN_BLOCKS) k_ensemble(Dev d, int iters, int init, int force_only) {
     // per-system prefix sums, [nsys + 1] each: particle offsets, warp items,
     // block items, active particles
     extern __shared__ unsigned s_dyn[];
@@ -539,6 +555,7 @@ __global__ void __launch_bounds__(THREADS) k_ensemble(Dev d, int iters, int init
     const bool from_state = init || (*d.forced_nact != 0u);
     const unsigned nthreads = gridDim.x * THREADS;
     const unsigned gtid = blockIdx.x * THREADS + threadIdx.x;
+    unsigned long long t_prev = (blockIdx.x == 0 && threadIdx.x == 0) ? device_ns() : 0ull;
     for (int it = 0; it < iters; it++) {
         // A: per system
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -548,6 +565,7 @@ __global__ void __launch_bounds__(THREADS) k_ensemble(Dev d, int iters, int init
         }
         for (int c = blockIdx.x; c < d.nsys; c += gridDim.x) phaseA<MODE>(d, c, init != 0, red, redd);
         if (!grid_sync(d)) return;
+        phase_mark(d, 0, t_prev);
         // prefix sums of the systems' counts
         unsigned c_off = 0, c_w = 0, c_b = 0, c_a = 0;
         for (int base = 0; base < d.nsys; base += THREADS) {
@@ -582,6 +600,7 @@ __global__ void __launch_bounds__(THREADS) k_ensemble(Dev d, int iters, int init
             predict_one<MODE>(d, S, g, from_state);
         }
         if (!grid_sync(d)) return;
+        phase_mark(d, 1, t_prev);
         // C: force sums
         if (MODE == H4_FORCE_MIXED) {
             const unsigned total_b = c_b;
@@ -606,6 +625,7 @@ __global__ void __launch_bounds__(THREADS) k_ensemble(Dev d, int iters, int init
             force_item<MODE>(d, d.sys[c], item - s_prefix[c], lane);
         }
         if (!grid_sync(d)) return;
+        phase_mark(d, 2, t_prev);
         if (force_only) return;
         // D: corrector of every active particle; the partial forces of
         // systems with many j-chunks are summed by a warp per particle
@@ -629,6 +649,7 @@ __global__ void __launch_bounds__(THREADS) k_ensemble(Dev d, int iters, int init
             correct_one(d, S, k, init != 0, fn);
         }
         if (!grid_sync(d)) return;
+        phase_mark(d, 3, t_prev);
         if (init) {
             // Hermite4::init_dt's CTIME and the first loop condition
             for (int c = blockIdx.x; c < d.nsys; c += gridDim.x) {
@@ -947,6 +968,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     EA(d.t, total); EA(d.dt, total); EA(d.move, total); EA(d.part, part_total);
     EA(d.queue, 1); EA(d.queue_b, 1); EA(d.bar_count, 1); EA(d.bar_gen, 1); EA(d.err, 2);
     EA(d.tune_ig, NB_N * NB_A); EA(d.tune_chunk, NB_N * NB_A); EA(d.forced_nact, 1); EA(d.launches, 1);
+    EA(d.phase_ns, 4);
     EA(d.epot_i, total); EA(d.energy, 2 * nsys);
     if (mode == H4_FORCE_MIXED) { EA(d.jf0, total); EA(d.jf1, total); EA(d.jf2, total); EA(d.jd, 5 * total); }
 #undef EA
@@ -975,6 +997,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     if (e == cudaSuccess) e = cudaMemsetAsync(d.err, 0, 8, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.forced_nact, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.launches, 0, 8, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.phase_ns, 0, 32, s);
     // persistent grid: every block resident (cooperative launch)
     E->smem = sizeof(unsigned) * 4 * (nsys + 1);
     int per_sm = 0;
@@ -1167,6 +1190,15 @@ int h4_ens_tune_force(h4_ens_handle E, unsigned int nact, unsigned int ig, unsig
     unsigned err = 0;
     ENS_TRY(cudaMemcpy(&err, E->d.err, 4, cudaMemcpyDeviceToHost), "error word");
     if (err) return efail(H4_ERR_CUDA, "h4_ens_tune_force: device error bits " + std::to_string(err));
+    return H4_OK;
+}
+
+int h4_ens_phase_times(h4_ens_handle E, double ms[4]) {
+    if (!E || !ms) return efail(H4_ERR_ARG, "h4_ens_phase_times: null argument");
+    unsigned long long ns[4];
+    ENS_TRY(cudaStreamSynchronize(E->stream), "h4_ens_phase_times");
+    ENS_TRY(cudaMemcpy(ns, E->d.phase_ns, sizeof(ns), cudaMemcpyDeviceToHost), "phase timers");
+    for (int k = 0; k < 4; k++) ms[k] = ns[k] * 1e-6;
     return H4_OK;
 }
 

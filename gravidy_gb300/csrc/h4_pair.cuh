@@ -9,15 +9,20 @@
 #pragma once
 #include "h4_internal.cuh"
 
-// j-loop unroll of the FP64 warp items (a build knob; 1 = as measured).
+// j-loop unroll of the FP64 and mixed warp items (build knobs, defaults as
+// measured best on GB300: 1 and 2).
 #ifndef H4_FP64_JUNROLL
 #define H4_FP64_JUNROLL 1
+#endif
+#ifndef H4_MIXED_JUNROLL
+#define H4_MIXED_JUNROLL 2
 #endif
 
 namespace h4 {
 namespace pair {
 
 constexpr int kFp64JUnroll = H4_FP64_JUNROLL;
+constexpr int kMixedJUnroll = H4_MIXED_JUNROLL;
 
 // 1/sqrt(x) in FP64: hardware reciprocal-square-root approximation
 // (rsqrt.approx.f64) refined by one cubic Householder step,
@@ -288,6 +293,7 @@ __device__ __forceinline__ void mixed_warp_item(const float4 *__restrict__ jf0, 
 #pragma unroll
             for (int c = 0; c < 6; c++) part[q][c] = 0.f;
         const int jl = min(j_end, jb + 32 * 16);
+#pragma unroll kMixedJUnroll
         for (int j = jb + lane; j < jl; j += 32) {
             const float4 j0 = jf0[j], j1 = jf1[j], j2 = jf2[j];
 #pragma unroll

@@ -123,3 +123,11 @@ class Ensemble:
         ms = C.c_float(); n = C.c_ulonglong()
         _lib.check_ens(self.L.h4_ens_timings(self.h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    PHASES = ("active_set", "prediction", "grav", "correction")
+
+    def phase_times(self) -> dict:
+        """Device ms per phase of the persistent kernel since creation."""
+        ms = np.zeros(4)
+        _lib.check_ens(self.L.h4_ens_phase_times(self.h, ms.ctypes.data))
+        return dict(zip(self.PHASES, ms.tolist()))

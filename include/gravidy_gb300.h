@@ -227,6 +227,11 @@ int h4_ens_tune_force(h4_ens_handle e, unsigned int nact, unsigned int ig,
                       unsigned int chunk, float *ms);
 int h4_ens_timings(h4_ens_handle e, float *advance_ms,
                    unsigned long long *kernel_launches);
+/* Device time per phase of the persistent ensemble kernel since creation
+ * (ms): 0 next block time + active sets + work layout (per system), 1
+ * predictor, 2 force sums, 3 reduction + corrector; read on the device clock
+ * at the grid barriers between phases. */
+int h4_ens_phase_times(h4_ens_handle e, double ms[4]);
 
 /* Force sum that allocates nothing.  No counterpart in the reference.
  *
