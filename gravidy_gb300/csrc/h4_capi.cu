@@ -40,9 +40,9 @@ int cuda_fail(cudaError_t e, const char *what) {
 // (measured on GB300: at N = 65536 the tiled kernel is faster from N_act ~ 64,
 // at N = 16384 from ~ 256).
 // Measured crossover of the two mixed kernels on GB300 (force kernel time,
-// N = 32768 .. 2^20): the warp items win below about 1000 active particles at
-// N = 32768, 450 at N = 65536 and 300-330 at N = 262144 and 2^20.
-unsigned default_mixed_threshold(unsigned n) { return n >= 65536u ? 384u : 768u; }
+// N = 32768 .. 2^20): the warp items win below about 700 active particles at
+// N = 32768, 300 at N = 65536 and 160-250 at N = 262144 and 2^20.
+unsigned default_mixed_threshold(unsigned n) { return n >= 131072u ? 192u : (n >= 65536u ? 320u : 768u); }
 
 bool is_pow2(double x) {
     if (!(x > 0.0) || !std::isfinite(x)) return false;

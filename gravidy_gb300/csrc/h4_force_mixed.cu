@@ -17,13 +17,15 @@
 // padded to a multiple of 256 with zero-mass particles (exact zero terms).
 //
 // Two shapes, chosen per launch from the active count:
-//  * tiled: a block owns 512 active particles (4 per thread, lanes over i)
-//    and one j-chunk; the chunk streams through shared memory in tiles of 256
-//    j, each tile brought in by three TMA bulk copies (cp.async.bulk) that
-//    complete on an mbarrier, double buffered;
+//  * tiled: a block owns a group of active particles (lanes over i) and one
+//    j-chunk; the chunk streams through shared memory in tiles of 256 j,
+//    each tile brought in by TMA bulk copies (cp.async.bulk) that complete on
+//    an mbarrier, double buffered.  The packed form (e2 > 0) holds two active
+//    particles per thread in f32x2 registers (256 per block); the scalar form
+//    (e2 = 0, explicit self mask) four per thread;
 //  * warp items (small active sets): a warp owns up to 4 active particles and
 //    one j-chunk, its lanes take interleaved j straight from L2, and the lane
-//    sums are combined with a shuffle tree in FP64.
+//    sums are combined by a reduce-scatter in double-single FP32.
 // Every wait on an mbarrier is bounded; on timeout the block records
 // H4_ERRBIT_TIMEOUT in the control block and leaves.
 #include <stdint.h>
@@ -92,9 +94,9 @@ struct MixedSplit {
 };
 
 // j-split of the tiled shape: chunks are whole tiles of the padded arrays.
-__device__ __forceinline__ MixedSplit tiled_split(const H4Dev &d, unsigned nact, unsigned blocks) {
+__device__ __forceinline__ MixedSplit tiled_split(const H4Dev &d, unsigned nact, unsigned blocks, unsigned ti) {
     MixedSplit s;
-    s.n_groups = (nact + TI - 1) / TI;
+    s.n_groups = (nact + ti - 1) / ti;
     unsigned split = (blocks * 6 + s.n_groups - 1) / s.n_groups;
     const unsigned tiles = (unsigned)(d.n_pad / JT);
     if (split > tiles) split = tiles;
@@ -129,7 +131,7 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled(H4Dev d, unsigned t
     __shared__ unsigned s_item;
     const unsigned nact = d.ctrl->nact;
     if (nact == 0 || nact < threshold) return;   // the warp-item kernel takes small sets
-    const MixedSplit sp = tiled_split(d, nact, gridDim.x);
+    const MixedSplit sp = tiled_split(d, nact, gridDim.x, TI);
     const int tid = threadIdx.x;
     if (blockIdx.x == 0 && tid == 0) {
         d.ctrl->force_split = sp.split;
@@ -253,16 +255,33 @@ __device__ __forceinline__ void lds2(const float4 *p, f2 &a, f2 &b) {
     asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(smem_addr(p)));
 }
 
-constexpr int IPT2 = 4;            // active particles per thread (2 packed pairs)
-constexpr int NPK = IPT2 / 2;
+// Shape of the packed kernel (build knobs; defaults as measured best on GB300):
+// packed pairs of active particles per thread, j-loop unroll, blocks per SM.
+// Measured (N = 16384 .. 2^20): one packed pair per thread at 4 blocks per SM
+// (120 registers, 16 warps per SM) beats two pairs at 3 blocks (168
+// registers, 12 warps) by 10-16 %: the FMA pipe's latency is hidden by more
+// warps better than by more independent pairs per warp.
+#ifndef H4_X2_NPK
+#define H4_X2_NPK 1
+#endif
+#ifndef H4_X2_UNROLL
+#define H4_X2_UNROLL 16
+#endif
+#ifndef H4_X2_BPS
+#define H4_X2_BPS 4
+#endif
+constexpr int NPK = H4_X2_NPK;
+constexpr int IPT2 = 2 * NPK;      // active particles per thread
+constexpr int TI2 = MT * IPT2;     // active particles per tile item
+constexpr int kX2Unroll = H4_X2_UNROLL;
 
-__global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled_x2(H4Dev d, unsigned threshold) {
+__global__ void __launch_bounds__(MT, H4_X2_BPS) k_force_mixed_tiled_x2(H4Dev d, unsigned threshold) {
     __shared__ __align__(128) float4 sj[2][5][JT];
     __shared__ __align__(8) uint64_t full[2];
     __shared__ unsigned s_item;
     const unsigned nact = d.ctrl->nact;
     if (nact == 0 || nact < threshold) return;
-    const MixedSplit sp = tiled_split(d, nact, gridDim.x);
+    const MixedSplit sp = tiled_split(d, nact, gridDim.x, TI2);
     const int tid = threadIdx.x;
     if (blockIdx.x == 0 && tid == 0) {
         d.ctrl->force_split = sp.split;
@@ -295,7 +314,7 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled_x2(H4Dev d, unsigne
         f2 S[NPK][6], Cc[NPK][6];
 #pragma unroll
         for (int q = 0; q < NPK; q++) {
-            const unsigned k0 = g * TI + tid + (2 * q) * MT, k1 = k0 + MT;
+            const unsigned k0 = g * TI2 + tid + (2 * q) * MT, k1 = k0 + MT;
             const IParticle a = load_i(d, checked_move(d, k0 < nact ? k0 : nact - 1));
             const IParticle b = load_i(d, checked_move(d, k1 < nact ? k1 : nact - 1));
             ip[q].xh = pk2(a.xh, b.xh); ip[q].yh = pk2(a.yh, b.yh); ip[q].zh = pk2(a.zh, b.zh);
@@ -333,7 +352,7 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled_x2(H4Dev d, unsigne
                 for (int q = 0; q < NPK; q++)
 #pragma unroll
                     for (int c = 0; c < 6; c++) part[q][c] = 0ull;
-#pragma unroll 4
+#pragma unroll kX2Unroll
                 for (int jj = sb; jj < sb + SUB; jj++) {
                     f2 jxh, jyh, jzh, jm, jxl, jyl, jzl, jvx, jvy, jvz;
                     lds2(&sj[b][0][jj], jxh, jyh);
@@ -363,7 +382,7 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled_x2(H4Dev d, unsigne
         double *p = d.part + (size_t)s * 6 * nact;
 #pragma unroll
         for (int q = 0; q < NPK; q++) {
-            const unsigned k0 = g * TI + tid + (2 * q) * MT, k1 = k0 + MT;
+            const unsigned k0 = g * TI2 + tid + (2 * q) * MT, k1 = k0 + MT;
 #pragma unroll
             for (int c = 0; c < 6; c++) {
                 if (k0 < nact) p[(size_t)c * nact + k0] = (double)lo2(S[q][c]) - (double)lo2(Cc[q][c]);
@@ -445,7 +464,7 @@ int launch_force_mixed(const H4Dev &d, int num_sms, unsigned threshold, long lon
         if (mask)
             k_force_mixed_tiled<true><<<num_sms * 3, MT, 0, s>>>(d, threshold);
         else if (d.jd)
-            k_force_mixed_tiled_x2<<<num_sms * 3, MT, 0, s>>>(d, threshold);
+            k_force_mixed_tiled_x2<<<num_sms * H4_X2_BPS, MT, 0, s>>>(d, threshold);
         else
             k_force_mixed_tiled<false><<<num_sms * 3, MT, 0, s>>>(d, threshold);
         launched++;

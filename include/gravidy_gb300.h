@@ -94,7 +94,8 @@ int h4_set_dt_limits(h4_handle h, double dt_min, double dt_max);
 int h4_set_force_mode(h4_handle h, int mode);
 /* H4_FORCE_MIXED: active-set size from which the shared-memory tiled kernel
  * (lanes over active particles) is used instead of warp items (lanes over j).
- * Default 384 for N >= 65536, else 768 (measured crossover on GB300). */
+ * Default 192 for N >= 131072, 320 for N >= 65536, else 768 (measured
+ * crossover on GB300). */
 int h4_set_mixed_threshold(h4_handle h, unsigned int nact_threshold);
 
 /* Hermite4GPU::init_acc_jrk (Hermite4GPU.cu:333-375): acc and jerk of all
