@@ -10,7 +10,7 @@
 //   A  per system (one block): next block time (min t + dt), the reference's
 //      loop condition, ordered active set, force work layout for its
 //      (N, N_act): warp items from the tuning table, or block-tiled items
-//      (mixed form, N_act >= 512);
+//      (mixed form, N_act >= BLOCK_MIN_NACT);
 //   B  all threads: predictor of every particle of the stepping systems;
 //   C  all blocks: the force sums -- block-tiled items (shared-memory j tiles,
 //      packed f32x2) then warp items, each from one global work queue (the
@@ -52,7 +52,10 @@ constexpr int NB_A = H4_ENS_TUNE_NB_A;
 constexpr unsigned long long BARRIER_TIMEOUT_NS = 60ull * 1000000000ull;
 constexpr int ITERS_PER_LAUNCH = 16;
 constexpr unsigned MAX_SYSTEMS = 4096;
-constexpr unsigned BLOCK_MIN_NACT = 512;   // mixed form: block-tiled items from this N_act
+#ifndef H4_ENS_BLOCK_MIN_NACT
+#define H4_ENS_BLOCK_MIN_NACT 2048
+#endif
+constexpr unsigned BLOCK_MIN_NACT = H4_ENS_BLOCK_MIN_NACT;   // mixed form: block-tiled items from this N_act
 constexpr int BTI = 2 * THREADS;           // active particles per block item (one packed pair per thread)
 constexpr int BJT = 256;                   // j per shared-memory tile of a block item
 constexpr int BCHUNK = 2048;               // j per block item

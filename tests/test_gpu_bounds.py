@@ -6,7 +6,7 @@ partial-force area, ensemble system ranges) and a violation fails the call
 instead of reading or writing out of bounds.  tests/bounds_scenarios.py runs
 single systems in every force form and kernel shape, the allocation-free
 entry point, diagnostics and ensembles at N = 1, 2, 31, 33, 257, 513, 1000,
-1500 under both builds, in child processes; the checked build must report
+1500, 2500 under both builds, in child processes; the checked build must report
 no violation and give bit-identical results to the normal one.
 """
 import json

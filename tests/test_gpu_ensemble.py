@@ -128,7 +128,7 @@ def test_ensemble_energy_matches_oracle():
 
 def test_ensemble_mixed_forces_vs_oracle():
     """Initial forces of every system (all particles active: block-tiled items
-    for N >= 512, warp items below) within the mixed-form tolerance."""
+    for N >= 2048, warp items below) within the mixed-form tolerance."""
     from h4_util import rel_err_vec
     systems = _systems([300, 700, 2048, 5000], seed0=1100)
     with Ensemble(systems, mode="mixed") as E:
