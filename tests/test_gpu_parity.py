@@ -220,3 +220,33 @@ def test_phase_timers_count_host_driven_calls():
         assert ph[k][0] > 0.0, k
     assert ph["energy"][1] == 1 and ph["advance"][1] == 1
     assert ph["grav"][0] <= ph["update"][0]
+
+
+@pytest.mark.parametrize("limits", [(2.0 ** -9, 2.0 ** -6), (2.0 ** -14, 2.0 ** -12)])
+def test_exact_mode_narrow_dt_limits_bit_exact(limits):
+    """Narrow timestep bounds (h4_set_dt_limits, D_TIME_MIN/D_TIME_MAX of
+    common.hpp:122,129) make most new timesteps hit a clamp of
+    NbodyUtils::normalize_dt (NbodyUtils.cpp:371-424) and of init_dt
+    (Hermite4.cpp:131-135); the exact mode still follows the oracle bit for
+    bit through both."""
+    dt_min, dt_max = limits
+    ns = golden_system("salpeter_n100")
+    o = oracle_for(ns, dt_min=dt_min, dt_max=dt_max)
+    o.init_acc_jrk()
+    oat = o.init_dt(0.0, float(orc.ETA_S))
+    with Hermite4GPU(ns, mode="exact", dt_min=dt_min, dt_max=dt_max) as g:
+        g.init_acc_jrk()
+        atime = g.init_dt(1.0e10, float(orc.ETA_S), 0.0)
+        assert atime == oat
+        assert np.array_equal(g.download()["dt"], o.dt)
+        oit = 0.0
+        clamped = 0
+        for step in range(120):
+            nact, itime, atime = g.step(atime)
+            onact, oit, oat = o.block_step(oit, oat)
+            assert (nact, itime, atime) == (onact, oit, oat), f"step {step}"
+            st = g.download()
+            assert np.array_equal(st["dt"], o.dt) and np.array_equal(st["t"], o.t), f"step {step}"
+            assert np.array_equal(st["r"], o.r), f"step {step}"
+            clamped += int(np.sum((o.dt == dt_min) | (o.dt == dt_max)))
+        assert clamped > 0   # the clamps were exercised
