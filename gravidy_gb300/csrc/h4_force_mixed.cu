@@ -250,9 +250,21 @@ using pair::IPair;
 using pair::kahan2;
 using pair::pair_x2;
 
-// 128-bit shared load as two packed operands
+// 128-bit shared load as two packed operands.  A plain load lets the
+// compiler fold the tile offsets into the instruction and schedule the loads
+// of the unrolled j loop freely (build knob H4_X2_ASM_LDS=1: the inline-PTX
+// form, kept for comparison).
+#ifndef H4_X2_ASM_LDS
+#define H4_X2_ASM_LDS 0
+#endif
 __device__ __forceinline__ void lds2(const float4 *p, f2 &a, f2 &b) {
+#if H4_X2_ASM_LDS
     asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(smem_addr(p)));
+#else
+    const ulonglong2 q = *reinterpret_cast<const ulonglong2 *>(p);
+    a = q.x;
+    b = q.y;
+#endif
 }
 
 // Shape of the packed kernel (build knobs; defaults as measured best on GB300):
