@@ -142,3 +142,20 @@ def test_ensemble_mixed_forces_vs_oracle():
         ej = rel_err_vec(got[:, 3:], want[:, 3:])
         assert np.median(ea) < 1e-6 and ea.max() < 1e-4, (c, np.median(ea), ea.max())
         assert np.median(ej) < 1e-6 and ej.max() < 1e-3, (c, np.median(ej), ej.max())
+
+
+def test_ensemble_phase_timers():
+    """Device time per phase of the persistent kernel (h4_ens_phase_times):
+    every phase ran, and the phases add up to no more than the advance's
+    CUDA-event time."""
+    systems = _systems([600, 2100, 900], seed0=1300)
+    with Ensemble(systems, mode="mixed") as E:
+        E.init()
+        p0 = E.phase_times()
+        E.advance(0.03125)
+        ms, _ = E.timings()
+        p1 = E.phase_times()
+    d = {k: p1[k] - p0[k] for k in p1}
+    assert list(d) == ["active_set", "prediction", "grav", "correction"]
+    assert all(v > 0.0 for v in d.values()), d
+    assert sum(d.values()) <= ms * 1.02 + 0.05, (d, ms)
