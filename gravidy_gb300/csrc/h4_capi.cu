@@ -170,19 +170,22 @@ double bits_to_double_host(unsigned long long b) {
     return x;
 }
 
-// One block step, device-driven (no host values): find active -> predict ->
-// force -> reduce + save old + correct -> next time.
-void enqueue_step(h4_system_s *h, cudaStream_t s) {
-    launch_find_active(h->d, false, 0.0, s);
-    launch_predict(h->d, false, 0.0, s);
+// One block step, device-driven (no host values): active set + predictor ->
+// force -> reduce + save old + correct -> next time; inside the graph's loop
+// (cond given) the next-time kernel also does the loop's bookkeeping.
+void enqueue_step(h4_system_s *h, cudaStream_t s, const cudaGraphConditionalHandle *cond) {
+    launch_find_active_predict(h->d, s);
     launch_force(h, s);
     launch_correct(h->d, false, 0.0, true, s);
-    launch_next_time(h->d, false, s);
-    h->launches += 5;   // find (2 kernels) + predict + correct + next time
+    if (cond)
+        launch_next_time_bookkeeping(h->d, *cond, s);
+    else
+        launch_next_time(h->d, false, s);
+    h->launches += 4;   // active set + predictor (2 kernels), correct, next time
 }
 
 // Kernels in one captured block step (force kernels counted per mode).
-int step_kernel_count(const h4_system_s *h) { return 5 + (h->mode == H4_FORCE_MIXED ? 2 : 1); }
+int step_kernel_count(const h4_system_s *h) { return 4 + (h->mode == H4_FORCE_MIXED ? 2 : 1); }
 
 int build_graph(h4_system_s *h) {
     if (h->graph_exec && h->graph_mode == h->mode) return H4_OK;
@@ -204,8 +207,7 @@ int build_graph(h4_system_s *h) {
                                          cudaStreamCaptureModeThreadLocal),
            "begin capture");
     unsigned long long saved = h->launches;
-    enqueue_step(h, h->graph_stream);
-    launch_advance_bookkeeping(h->d, cond, true, h->graph_stream);
+    enqueue_step(h, h->graph_stream, &cond);
     h->launches = saved;
     cudaGraph_t captured = nullptr;
     cudaError_t e = cudaStreamEndCapture(h->graph_stream, &captured);
@@ -507,7 +509,7 @@ int h4_step(h4_handle h, double *atime, double *itime, unsigned int *nact) {
     if (!h) return fail(H4_ERR_ARG, "null handle");
     if (!h->forces_ready) return fail(H4_ERR_STATE, "h4_step: call h4_init_acc_jrk and h4_init_dt first");
     if (atime) { launch_set_atime(h->d, *atime, h->stream); h->launches += 1; }
-    enqueue_step(h, h->stream);
+    enqueue_step(h, h->stream, nullptr);
     int st = check_launch("h4_step");
     if (st) return st;
     if (atime || itime || nact) {
@@ -552,7 +554,7 @@ int h4_advance(h4_handle h, double t_stop, double t_log, double *atime, double *
     h->phase[PH_ADVANCE].total_ms += h->last_advance_ms;
     h->phase[PH_ADVANCE].count += 1;
     const H4Ctrl &o = *h->h_ctrl;
-    h->launches += (unsigned long long)o.steps * (unsigned long long)(step_kernel_count(h) + 1);
+    h->launches += (unsigned long long)o.steps * (unsigned long long)step_kernel_count(h);
     if (atime) *atime = bits_to_double_host(o.atime_bits);
     if (itime) *itime = o.itime;
     if (stats) {

@@ -152,16 +152,17 @@ void launch_predict(const H4Dev &d, bool host_itime, double itime, cudaStream_t 
 void launch_reduce_forces(const H4Dev &d, bool save_old, cudaStream_t s);
 void launch_correct(const H4Dev &d, bool host_itime, double itime, bool fused_reduce, cudaStream_t s);
 void launch_next_time(const H4Dev &d, bool reset, cudaStream_t s);
+// Device-resident step: active set + predictor in the first pass (2 kernels),
+// and the next block time with the loop's bookkeeping (1 kernel).
+void launch_find_active_predict(const H4Dev &d, cudaStream_t s);
+void launch_next_time_bookkeeping(const H4Dev &d, cudaGraphConditionalHandle cond, cudaStream_t s);
 void launch_init_dt(const H4Dev &d, float eta, double itime, cudaStream_t s);
-void launch_advance_bookkeeping(const H4Dev &d, cudaGraphConditionalHandle cond, bool use_cond,
-                                cudaStream_t s);
 void launch_identity_move(const H4Dev &d, cudaStream_t s);
 void launch_set_nact(const H4Dev &d, unsigned nact, cudaStream_t s);
 void launch_set_atime(const H4Dev &d, double atime, cudaStream_t s);
 void launch_reduce_to(const H4Dev &d, double *out, cudaStream_t s);
 void launch_set_pred_from_state(const H4Dev &d, cudaStream_t s);
 void launch_pad_predicted(const H4Dev &d, cudaStream_t s);
-int kernels_per_step();
 
 // ---- force kernels -----------------------------------------------------------
 // Active list and count come from d.move / d.ctrl->nact; results are written

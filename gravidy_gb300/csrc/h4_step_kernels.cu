@@ -88,9 +88,7 @@ __device__ __forceinline__ void write_jf(const H4Dev &d, int i, const dbl4 &pr, 
 
 // ---- active set (Hermite4::find_particles_to_move) --------------------------
 // Pass 1: active count of each chunk of FLAG_CHUNK particles.
-__global__ void __launch_bounds__(FLAG_THREADS)
-k_flag_count(H4Dev d, int host_itime, double itime_in) {
-    double itime = host_itime ? itime_in : bits_to_double(d.ctrl->atime_bits);
+__device__ __forceinline__ void flag_count_chunk(const H4Dev &d, double itime) {
     const int base = blockIdx.x * FLAG_CHUNK + threadIdx.x * FLAG_ITEMS;
     unsigned c = 0;
 #pragma unroll
@@ -103,6 +101,11 @@ k_flag_count(H4Dev d, int host_itime, double itime_in) {
         d.blk_cnt[blockIdx.x] = c;
         if (blockIdx.x == 0) d.ctrl->itime = itime;
     }
+}
+
+__global__ void __launch_bounds__(FLAG_THREADS)
+k_flag_count(H4Dev d, int host_itime, double itime_in) {
+    flag_count_chunk(d, host_itime ? itime_in : bits_to_double(d.ctrl->atime_bits));
 }
 
 // Pass 2: ordered scatter of the active indices (ascending i, as the
@@ -150,15 +153,30 @@ __global__ void k_save_old(H4Dev d) {
 }
 
 // ---- Hermite4CPU::predicted_pos_vel (Hermite4CPU.cpp:340-365) ---------------
-__global__ void __launch_bounds__(256) k_predict(H4Dev d, int host_itime, double itime_in) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.n) return;
-    const double itime = host_itime ? itime_in : d.ctrl->itime;
+__device__ __forceinline__ void predict_particle(const H4Dev &d, int i, double itime) {
     dbl4 pr, pv;
     exact::predict(itime, d.t[i], d.f + 6 * (size_t)i, d.r[i], d.v[i], pr, pv);
     d.pr[i] = pr;
     d.pv[i] = pv;
     if (d.jf0) write_jf(d, i, pr, pv);
+}
+
+__global__ void __launch_bounds__(256) k_predict(H4Dev d, int host_itime, double itime_in) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    predict_particle(d, i, host_itime ? itime_in : d.ctrl->itime);
+}
+
+// The device-resident step's first pass: the active counts of the chunks
+// (the first nb_flag blocks, one chunk each) and the predictor of every
+// particle at the next block time (the control block's atime; one particle
+// per thread, all blocks), in one launch.  Same arithmetic as k_flag_count
+// then k_predict.
+__global__ void __launch_bounds__(FLAG_THREADS) k_flag_count_predict(H4Dev d, int nb_flag) {
+    const double itime = bits_to_double(d.ctrl->atime_bits);
+    if ((int)blockIdx.x < nb_flag) flag_count_chunk(d, itime);
+    const int i = blockIdx.x * FLAG_THREADS + threadIdx.x;
+    if (i < d.n) predict_particle(d, i, itime);
 }
 
 // Predictors straight from the state (Hermite4::init_data, Hermite4.cpp:
@@ -286,7 +304,12 @@ __global__ void __launch_bounds__(128) k_correct(H4Dev d, int host_itime, double
 // ---- Hermite4::next_integration_time (Hermite4.cpp:90-102) ------------------
 __global__ void k_reset_atime(H4Dev d) { d.ctrl->atime_bits = INF_BITS; }
 
-__global__ void __launch_bounds__(256) k_next_time(H4Dev d) {
+__device__ void advance_bookkeeping(const H4Dev &d, cudaGraphConditionalHandle cond, int use_cond);
+
+// bookkeep: also the per-step bookkeeping of the device-resident loop (one
+// thread), which needs nothing this kernel computes.
+__global__ void __launch_bounds__(256) k_next_time(H4Dev d, int bookkeep, cudaGraphConditionalHandle cond) {
+    if (bookkeep && blockIdx.x == 0 && threadIdx.x == 0) advance_bookkeeping(d, cond, 1);
     double m = __longlong_as_double((long long)INF_BITS);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x)
         m = fmin(m, add(d.t[i], d.dt[i]));
@@ -333,7 +356,7 @@ __global__ void k_reduce_to(H4Dev d, double *out) {
 }
 
 // ---- per-step bookkeeping of the device-resident loop ------------------------
-__global__ void k_advance_bookkeeping(H4Dev d, cudaGraphConditionalHandle cond, int use_cond) {
+__device__ void advance_bookkeeping(const H4Dev &d, cudaGraphConditionalHandle cond, int use_cond) {
     H4Ctrl *c = d.ctrl;
     const unsigned nact = c->nact;
     c->steps += 1;
@@ -353,9 +376,8 @@ __global__ void k_advance_bookkeeping(H4Dev d, cudaGraphConditionalHandle cond, 
     if (use_cond) cudaGraphSetConditional(cond, go ? 1u : 0u);
 }
 
-}  // namespace
 
-int kernels_per_step() { return 6; }
+}  // namespace
 
 static inline int blocks_for(int n, int t) { return (n + t - 1) / t > 0 ? (n + t - 1) / t : 1; }
 
@@ -385,7 +407,20 @@ void launch_next_time(const H4Dev &d, bool reset, cudaStream_t s) {
     if (reset) k_reset_atime<<<1, 1, 0, s>>>(d);
     int nb = blocks_for(d.n, 256);
     if (nb > 1024) nb = 1024;
-    k_next_time<<<nb, 256, 0, s>>>(d);
+    k_next_time<<<nb, 256, 0, s>>>(d, 0, cudaGraphConditionalHandle{});
+}
+
+void launch_next_time_bookkeeping(const H4Dev &d, cudaGraphConditionalHandle cond, cudaStream_t s) {
+    int nb = blocks_for(d.n, 256);
+    if (nb > 1024) nb = 1024;
+    k_next_time<<<nb, 256, 0, s>>>(d, 1, cond);
+}
+
+void launch_find_active_predict(const H4Dev &d, cudaStream_t s) {
+    const int nb = blocks_for(d.n, FLAG_CHUNK);
+    const int np = blocks_for(d.n, FLAG_THREADS);   // >= nb
+    k_flag_count_predict<<<np, FLAG_THREADS, 0, s>>>(d, nb);
+    k_flag_scatter<<<nb, FLAG_THREADS, 0, s>>>(d, nb);
 }
 
 void launch_init_dt(const H4Dev &d, float eta, double itime, cudaStream_t s) {
@@ -413,9 +448,5 @@ void launch_reduce_to(const H4Dev &d, double *out, cudaStream_t s) {
     k_reduce_to<<<blocks_for(d.n, 256), 256, 0, s>>>(d, out);
 }
 
-void launch_advance_bookkeeping(const H4Dev &d, cudaGraphConditionalHandle cond, bool use_cond,
-                                cudaStream_t s) {
-    k_advance_bookkeeping<<<1, 1, 0, s>>>(d, cond, use_cond ? 1 : 0);
-}
 
 }  // namespace h4
