@@ -269,6 +269,7 @@ int h4_create(h4_handle *out, unsigned int n, double e2, float eta, const h4_dou
     d.dt_min = 1.1920928955078125e-07;
     d.dt_max = 0.125;
     h->mode = mode;
+    d.mixed = mode == H4_FORCE_MIXED ? 1 : 0;
     h->mixed_threshold = default_mixed_threshold(n);
     const size_t N = n, NP = (size_t)d.n_pad;
     d.part_cap = 6 * (N + 262144);
@@ -359,7 +360,14 @@ int h4_set_dt_limits(h4_handle h, double dt_min, double dt_max) {
 int h4_set_force_mode(h4_handle h, int mode) {
     if (!h) return fail(H4_ERR_ARG, "null handle");
     if (mode < H4_FORCE_FP64 || mode > H4_FORCE_MIXED) return fail(H4_ERR_ARG, "unknown force mode");
+    const int was_mixed = h->d.mixed;
     h->mode = mode;
+    h->d.mixed = mode == H4_FORCE_MIXED ? 1 : 0;
+    if (h->d.mixed && !was_mixed) {   // the FP32 j data of the current predictors
+        launch_pack_j(h->d, h->stream);
+        h->launches += 1;
+        return check_launch("h4_set_force_mode");
+    }
     return H4_OK;
 }
 
@@ -655,6 +663,10 @@ int h4_forces_for(h4_handle h, const h4_double4 *pr, const h4_double4 *pv, unsig
     H4_TRY(cudaMemcpyAsync(h->d.pr, pr, N * 32, cudaMemcpyHostToDevice, s), "h4_forces_for pr");
     H4_TRY(cudaMemcpyAsync(h->d.pv, pv, N * 32, cudaMemcpyHostToDevice, s), "h4_forces_for pv");
     H4_TRY(cudaMemcpyAsync(h->d.move, move, (size_t)nact * 4, cudaMemcpyHostToDevice, s), "h4_forces_for move");
+    if (h->d.mixed) {   // the mixed kernels read the FP32 j data of these predictors
+        launch_pack_j(h->d, s);
+        h->launches += 1;
+    }
     int st = set_nact(h, nact);
     if (st) return st;
     cudaEventRecord(h->ev0, s);

@@ -127,6 +127,7 @@ struct H4Dev {
     float4 *jd;              // [5][n_pad] the same j data with every value twice, for
                              // packed f32x2 arithmetic: (xh,xh,yh,yh), (zh,zh,m,m),
                              // (xl,xl,yl,yl), (zl,zl,vx,vx), (vy,vy,vz,vz)
+    int mixed;              // mixed form selected: the predictor also writes jf0..2 and jd
     unsigned int *move;     // [n] active list
     unsigned int *blk_cnt;  // [n_blocks_flag] active count per chunk
     double *part;           // partial forces, [S][6][nact] for the current step
@@ -163,6 +164,8 @@ void launch_set_atime(const H4Dev &d, double atime, cudaStream_t s);
 void launch_reduce_to(const H4Dev &d, double *out, cudaStream_t s);
 void launch_set_pred_from_state(const H4Dev &d, cudaStream_t s);
 void launch_pad_predicted(const H4Dev &d, cudaStream_t s);
+// The mixed form's j data (jf0..2, jd) from the predicted arrays pr, pv.
+void launch_pack_j(const H4Dev &d, cudaStream_t s);
 
 // ---- force kernels -----------------------------------------------------------
 // Active list and count come from d.move / d.ctrl->nact; results are written

@@ -158,7 +158,7 @@ __device__ __forceinline__ void predict_particle(const H4Dev &d, int i, double i
     exact::predict(itime, d.t[i], d.f + 6 * (size_t)i, d.r[i], d.v[i], pr, pv);
     d.pr[i] = pr;
     d.pv[i] = pv;
-    if (d.jf0) write_jf(d, i, pr, pv);
+    if (d.mixed) write_jf(d, i, pr, pv);
 }
 
 __global__ void __launch_bounds__(256) k_predict(H4Dev d, int host_itime, double itime_in) {
@@ -189,7 +189,12 @@ __global__ void k_pred_from_state(H4Dev d) {
     v.w = 0.0;
     d.pr[i] = r;
     d.pv[i] = v;
-    if (d.jf0) write_jf(d, i, r, v);
+    if (d.mixed) write_jf(d, i, r, v);
+}
+
+__global__ void k_pack_j(H4Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d.n) write_jf(d, i, d.pr[i], d.pv[i]);
 }
 
 // Padding of the predicted arrays past n: zero mass, far away, at rest.
@@ -434,6 +439,10 @@ void launch_identity_move(const H4Dev &d, cudaStream_t s) {
 
 void launch_set_pred_from_state(const H4Dev &d, cudaStream_t s) {
     k_pred_from_state<<<blocks_for(d.n, 256), 256, 0, s>>>(d);
+}
+
+void launch_pack_j(const H4Dev &d, cudaStream_t s) {
+    k_pack_j<<<blocks_for(d.n, 256), 256, 0, s>>>(d);
 }
 
 void launch_pad_predicted(const H4Dev &d, cudaStream_t s) {

@@ -78,3 +78,54 @@ def test_mixed_c1_energy_error_within_2x_fp64():
         res[mode] = log.rows[-1][5]
     print("CumE at t=1:", res)
     assert res["mixed"] <= 2.0 * res["fp64"]
+
+
+@pytest.mark.parametrize("threshold", [1, 1 << 30])
+def test_mixed_forces_for_uses_the_given_predictors(threshold):
+    """h4_forces_for in the mixed form packs its FP32 j data from the
+    predictors it is given, not from the handle's last prediction: forces of
+    perturbed predictors (not the state the handle holds) match the oracle's
+    forces of the same predictors."""
+    n, nact = 4000, 700
+    ns = plummer_system(n, seed=12, imf="salpeter")
+    rng = np.random.default_rng(12)
+    pos = ns.pos + 1e-2 * rng.standard_normal(ns.pos.shape)
+    vel = ns.vel * 1.3
+    move = np.sort(rng.choice(n, size=nact, replace=False)).astype(np.uint32)
+    pr = np.zeros((n, 4)); pr[:, :3] = pos; pr[:, 3] = ns.mass
+    pv = np.zeros((n, 4)); pv[:, :3] = vel
+    want = orc.forces_for(orc.make_predictors(ns.mass, pos, vel), ns.e2, move)
+    with Hermite4GPU(ns, mode="mixed") as g:
+        g.set_mixed_threshold(threshold)
+        got = g.forces_for(pr, pv, move)
+    ea = rel_err_vec(got[:, :3], want[:, :3])
+    ej = rel_err_vec(got[:, 3:], want[:, 3:])
+    assert np.median(ea) < MIXED_MED_RTOL and ea.max() < MIXED_MAX_RTOL
+    assert np.median(ej) < MIXED_MED_RTOL and ej.max() < MIXED_MAX_RTOL
+
+
+def test_switch_to_mixed_packs_current_predictors():
+    """h4_set_force_mode into the mixed form between the methods of a block
+    step: the force sum uses the j data of the current predictors."""
+    ns = plummer_system(3000, seed=13, imf="salpeter")
+    with Hermite4GPU(ns, mode="fp64") as a, Hermite4GPU(ns, mode="mixed") as b:
+        for g in (a, b):
+            g.init_acc_jrk()
+        ta = a.init_dt()
+        tb = b.init_dt()
+        assert ta == tb
+        for g, t in ((a, ta), (b, tb)):
+            nact = g.find_particles_to_move(t)
+            g.save_old_acc_jrk(nact)
+            g.predicted_pos_vel(t)
+        _lib_set = a.L.h4_set_force_mode
+        assert _lib_set(a.h, 2) == 0     # fp64 -> mixed after the FP64-mode prediction
+        nact = a.find_particles_to_move(ta)
+        a.update_acc_jrk(nact)
+        b.update_acc_jrk(nact)
+        sa, sb = a.download(), b.download()
+    act = sa["move"][:nact]
+    assert np.array_equal(act, sb["move"][:nact])
+    # the active particles' new forces (the others keep their initial forces,
+    # FP64 in a and mixed in b)
+    assert np.array_equal(sa["f"][act], sb["f"][act])
