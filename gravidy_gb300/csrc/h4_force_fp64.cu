@@ -21,8 +21,9 @@
 //    y = y0 (1 + e/2 + 3e^2/8), e = 1 - r2 y0^2, which is accurate to the last
 //    bits of a double;
 //  * jerk as A (dv - 3 (dr.dv)/r2 dr): 31 FP64 instructions per pair;
-//  * the 32 lane sums are combined with a fixed shuffle tree, the j-chunks of
-//    one particle in chunk order by the reduction kernel: deterministic.
+//  * the lane sums are combined by a fixed butterfly reduce-scatter, the
+//    j-chunks of one particle in a fixed order by the reduction kernel:
+//    deterministic.
 // Work items are handed out through an atomic counter in the control block
 // (reset by the active-set kernel of the step).
 #include "h4_internal.cuh"

@@ -3,7 +3,8 @@
 //
 // A warp item is (up to 4 active particles, one j range): the 32 lanes take
 // interleaved j, every lane keeps the sums of all the item's particles, and a
-// fixed shuffle tree combines the lanes at the end (deterministic).  Results
+// fixed butterfly reduce-scatter combines the lanes at the end
+// (deterministic).  Results
 // go to part_s[c * nact + k] (component c of active particle k, for this
 // j-chunk).  Indices in `move` and j are relative to the arrays passed.
 #pragma once
@@ -270,7 +271,8 @@ __device__ __forceinline__ void pair_mixed(const IParticle &p, float4 j0, float4
 }
 
 // Mixed warp item: FP32 lane sums over runs of 16 j, Kahan-compensated
-// across runs, FP64 shuffle tree across lanes.
+// across runs, double-single reduce-scatter across lanes, one FP64 value per
+// lane at the end.
 template <int NI, bool MASK_SELF>
 __device__ __forceinline__ void mixed_warp_item(const float4 *__restrict__ jf0, const float4 *__restrict__ jf1,
                                                 const float4 *__restrict__ jf2, const unsigned *__restrict__ move,
