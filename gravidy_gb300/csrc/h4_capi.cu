@@ -36,10 +36,8 @@ int cuda_fail(cudaError_t e, const char *what) {
         if (e__ != cudaSuccess) return cuda_fail(e__, what); \
     } while (0)
 
-// Active-set size from which the tiled mixed kernel beats the warp items
-// (measured on GB300: at N = 65536 the tiled kernel is faster from N_act ~ 64,
-// at N = 16384 from ~ 256).
-// Measured crossover of the two mixed kernels on GB300 (force kernel time,
+// Active-set size from which the tiled mixed kernel is used instead of the
+// warp items.  Measured crossover of the two mixed kernels on GB300 (force kernel time,
 // N = 32768 .. 2^20): the warp items win below about 700 active particles at
 // N = 32768, 300 at N = 65536 and 160-250 at N = 262144 and 2^20.
 unsigned default_mixed_threshold(unsigned n) { return n >= 131072u ? 192u : (n >= 65536u ? 320u : 768u); }
