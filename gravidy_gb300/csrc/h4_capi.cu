@@ -120,15 +120,26 @@ void phase_resolve(PhaseTimer &p) {
     p.pending = false;
 }
 
+// Timers are best effort: a timer whose events cannot be created stays off,
+// and its failure is cleared so that it never surfaces as the error of the
+// call it times.
 void phase_begin(h4_system_s *h, Phase ph) {
     PhaseTimer &p = h->phase[ph];
     phase_resolve(p);
-    if (!p.a) { cudaEventCreate(&p.a); cudaEventCreate(&p.b); }
+    if (!p.a) {
+        if (cudaEventCreate(&p.a) != cudaSuccess || cudaEventCreate(&p.b) != cudaSuccess) {
+            if (p.a) cudaEventDestroy(p.a);
+            p.a = p.b = nullptr;
+            cudaGetLastError();
+            return;
+        }
+    }
     cudaEventRecord(p.a, h->stream);
 }
 
 void phase_end(h4_system_s *h, Phase ph) {
     PhaseTimer &p = h->phase[ph];
+    if (!p.a) return;
     cudaEventRecord(p.b, h->stream);
     p.pending = true;
 }
