@@ -94,3 +94,45 @@ def test_plummer_is_seeded():
     c = ics.plummer(500, 10)
     assert all(np.array_equal(x, y) for x, y in zip(a, b))
     assert not np.array_equal(a[1], c[1])
+
+
+def _header_defines():
+    text = open(os.path.join(ROOT, "include", "gravidy_gb300.h")).read()
+    return {k: int(v) for k, v in re.findall(r"#define\s+(H4_[A-Z0-9_]+)\s+\(?(\d+)", text)}
+
+
+def test_header_constants_match_the_binding():
+    """Constants of include/gravidy_gb300.h used by the Python side."""
+    from gravidy_gb300 import ensemble
+    d = _header_defines()
+    assert d["H4_ENS_TUNE_NB_N"] == ensemble.NB_N and d["H4_ENS_TUNE_NB_A"] == ensemble.NB_A
+    assert d["H4_PHASES"] == 8 and d["H4_BUILD_BOUNDS_CHECK"] == 1
+    assert _lib.MODES == {"fp64": 0, "exact": 1, "mixed": 2}
+    L = _lib.load()
+    assert [L.h4_phase_name(k).decode() for k in range(d["H4_PHASES"])] == [
+        "prediction", "update", "grav", "correction", "active_set", "next_time", "energy", "advance"]
+    assert L.h4_phase_name(d["H4_PHASES"]) == b""
+    assert L.h4_build_flags() in (0, d["H4_BUILD_BOUNDS_CHECK"])
+
+
+def test_committed_tuning_table_is_well_formed():
+    """gravidy_gb300/tuning/ensemble_gb300.json: one (ig, chunk) table per
+    force form, NB_N x NB_A entries, ig in {1, 2, 4}, chunks multiples of 32."""
+    import json
+    from gravidy_gb300 import ensemble
+    t = json.load(open(ensemble.TUNING_FILE))
+    for mode in ("fp64", "mixed"):
+        ig = np.array(t["modes"][mode]["ig"])
+        ch = np.array(t["modes"][mode]["chunk"])
+        assert ig.shape == ch.shape == (ensemble.NB_N, ensemble.NB_A)
+        assert set(np.unique(ig)) <= {1, 2, 4}
+        assert np.all(ch >= 32) and np.all(ch % 32 == 0)
+
+
+def test_c4_sizes_are_seeded_and_in_range():
+    from gravidy_gb300 import workloads
+    a = workloads.c4_sizes(256, seed=7)
+    b = workloads.c4_sizes(256, seed=7)
+    assert np.array_equal(a, b) and len(a) == 256
+    assert a.min() >= 512 and a.max() <= 16384
+    assert not np.array_equal(a, workloads.c4_sizes(256, seed=8))
