@@ -36,6 +36,8 @@ def test_create_validates_arguments_before_touching_the_device():
     h = C.c_void_p()
     r = np.zeros((4, 4)); v = np.zeros((4, 4))
     assert L.h4_create(C.byref(h), 0, 1e-4, C.c_float(0.01), r.ctypes.data, v.ctypes.data, 0) == 1
+    assert L.h4_create(C.byref(h), (1 << 28) + 1, 1e-4, C.c_float(0.01), r.ctypes.data, v.ctypes.data, 0) == 1
+    assert b"2^28" in L.h4_last_error()
     assert L.h4_create(C.byref(h), 4, -1.0, C.c_float(0.01), r.ctypes.data, v.ctypes.data, 0) == 1
     assert L.h4_create(C.byref(h), 4, 1e-4, C.c_float(0.01), None, v.ctypes.data, 0) == 1
     assert L.h4_create(C.byref(h), 4, 1e-4, C.c_float(0.01), r.ctypes.data, v.ctypes.data, 7) == 1
