@@ -26,8 +26,9 @@
 //  * warp items (small active sets): a warp owns up to 4 active particles and
 //    one j-chunk, its lanes take interleaved j straight from L2, and the lane
 //    sums are combined by a reduce-scatter in double-single FP32.
-// Every wait on an mbarrier is bounded; on timeout the block records
-// H4_ERRBIT_TIMEOUT in the control block and leaves.
+// Every wait on an mbarrier is bounded; on timeout the block waits (bounded)
+// for its copies still in flight, records H4_ERRBIT_TIMEOUT in the control
+// block and leaves.
 #include <stdint.h>
 
 #include "h4_internal.cuh"
@@ -68,6 +69,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
         : "r"(smem_addr(bar)), "r"(parity)
         : "memory");
     return ok != 0;
+}
+
+// Timeout path of the double-buffered tile loop: before the block leaves,
+// wait (bounded again) for the copies it may still have in flight into its
+// shared memory -- the tile that timed out (global tile index gt) and the
+// one after it, if issued -- so that no bulk copy lands in the shared memory
+// of a block that has exited.
+__device__ __forceinline__ void drain_tiles(uint64_t *full, unsigned gt, int tiles_left) {
+    for (int k = 0; k < 2 && k < tiles_left; k++) {
+        const unsigned g = gt + (unsigned)k;
+        unsigned spins = 0;
+        while (!mbar_try_wait(&full[g & 1u], (g >> 1) & 1u) && ++spins < WAIT_LIMIT) {
+        }
+    }
 }
 
 // 1-D bulk copy global -> shared, completion counted on `bar` (16-byte
@@ -189,7 +204,10 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled(H4Dev d, unsigned t
                 if (++spins > WAIT_LIMIT) { ok = false; break; }
             }
             if (__syncthreads_or(!ok)) {
-                if (tid == 0) atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_TIMEOUT);
+                if (tid == 0) {
+                    drain_tiles(full, gt, ntiles - t);
+                    atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_TIMEOUT);
+                }
                 return;
             }
             const int jt0 = j_begin + t * JT;
@@ -354,7 +372,10 @@ __global__ void __launch_bounds__(MT, H4_X2_BPS) k_force_mixed_tiled_x2(H4Dev d,
                 if (++spins > WAIT_LIMIT) { ok = false; break; }
             }
             if (__syncthreads_or(!ok)) {
-                if (tid == 0) atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_TIMEOUT);
+                if (tid == 0) {
+                    drain_tiles(full, gt, ntiles - t);
+                    atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_TIMEOUT);
+                }
                 return;
             }
 #pragma unroll 1

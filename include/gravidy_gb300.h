@@ -238,9 +238,12 @@ int h4_ens_phase_times(h4_ens_handle e, double ms[4]);
  *
  * For callers that cannot call cudaMalloc -- an application that hands all
  * of the GPU's memory to its own pool at start-up, or a time-critical loop
- * that cannot take the synchronisation an allocation may imply.  Same result
- * as h4_forces_for (FP64 kernel, same split and summation order), but every
- * buffer is the caller's device memory and no handle is needed:
+ * that cannot take the synchronisation an allocation may imply.  The FP64
+ * force kernel; it agrees with h4_forces_for of an FP64-mode handle to within
+ * rounding (for large nact the j-split, and so the summation order, may
+ * differ, since the scratch is smaller than a handle's), but every buffer is
+ * the caller's device memory and no handle is needed:
+ *   n           particles, 1 .. 2^28 (the limit of h4_create)
  *   d_pr, d_pv  n predicted positions (w = mass) and velocities, 32-byte
  *               aligned device arrays of h4_double4
  *   d_move      nact particle indices (device), d_out nact h4_forces (device)
@@ -248,10 +251,13 @@ int h4_ens_phase_times(h4_ens_handle e, double ms[4]);
  * The partial sums use a fixed file-scope device array of
  * H4_NOALLOC_SCRATCH_DOUBLES doubles (16 MiB), held on every GPU that loads
  * this library until the process exits; nact above H4_NOALLOC_MAX_NACT is
- * rejected with H4_ERR_ARG.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  Calls share the array:
- * calls that overlap on the GPU race and must be serialised by the caller.
+ * rejected with H4_ERR_ARG.  The first call on a device is its set-up: it
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current, which may load the library's device code there; make that
+ * first call before any stream capture.  Later calls repeat the cheap
+ * look-up.  Calls share the array, and each call clears the part of it that
+ * must start at zero: calls that overlap on the GPU race and must be
+ * serialised by the caller.
  * The call is asynchronous on `stream`; the message of a failure is
  * returned by h4_forces_noalloc_error(). */
 #define H4_NOALLOC_SCRATCH_DOUBLES (2u * 1024u * 1024u)

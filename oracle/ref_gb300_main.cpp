@@ -1,6 +1,6 @@
 /* The reference program's main (src/gravidy.cpp:54-115) with the GB300
  * backend class Hermite4GB300 in place of Hermite4GPU -- what the reference's
- * main becomes with the one-line branch of INTEGRATION.md.  Test
+ * main becomes when its GPU branch constructs Hermite4GB300 instead.  Test
  * infrastructure: it shows the adapter compiles and links against the
  * reference's own classes (make -C oracle adapter); the reference's
  * gravidy.cpp itself is not modified. */

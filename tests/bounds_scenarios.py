@@ -97,6 +97,37 @@ def noalloc(n, seed):
     return _h(*outs)
 
 
+def noalloc_recovers(n, seed):
+    """Bounds-checked build only: a call whose active list names a particle
+    past n fails with H4_ERR_STATE (the kernels' own checks skip the access),
+    and the next call with a valid list succeeds and matches a fresh one --
+    the failure does not stick to the shared control block."""
+    import torch
+    ns = _system(n, seed)
+    pr = np.zeros((n, 4)); pr[:, :3] = ns.pos; pr[:, 3] = ns.mass
+    pv = np.zeros((n, 4)); pv[:, :3] = ns.vel
+    L = _lib.load()
+    dev = torch.device("cuda", 0)
+    d_pr, d_pv = torch.from_numpy(pr).to(dev), torch.from_numpy(pv).to(dev)
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+    def call(move):
+        d_move = torch.from_numpy(move.astype(np.int32)).to(dev)
+        d_out = torch.zeros((len(move), 6), dtype=torch.float64, device=dev)
+        st = L.h4_forces_noalloc(n, ns.e2, C.c_void_p(d_pr.data_ptr()), C.c_void_p(d_pv.data_ptr()), len(move),
+                                 C.c_void_p(d_move.data_ptr()), C.c_void_p(d_out.data_ptr()), stream)
+        torch.cuda.synchronize()
+        return st, d_out.cpu().numpy()
+
+    good = np.arange(0, n, 3, dtype=np.uint32)
+    st0, want = call(good)
+    bad = good.copy()
+    bad[len(bad) // 2] = n + 5
+    st1, _ = call(bad)
+    st2, got = call(good)
+    return st0 == 0 and st1 == 4 and st2 == 0 and np.array_equal(got, want)
+
+
 def ensemble(mode, sizes, t_end, seed0=300):
     systems = []
     for k, n in enumerate(sizes):
@@ -134,6 +165,10 @@ def main():
     sizes = [2, 33, 257, 513, 1000, 1500, 2500]   # 2500: block-tiled items at init (mixed)
     for mode in ("fp64", "mixed", "exact"):
         R[f"ensemble_{mode}"] = ensemble(mode, sizes if mode != "exact" else sizes[:4], 2.0 ** -5)[0]
+    if out["build_flags"] & 1:
+        # failure paths that only the checked build can take without an
+        # out-of-bounds access
+        out["checked_only"] = {"noalloc_recovers": bool(noalloc_recovers(1000, 77))}
     print(json.dumps(out))
 
 

@@ -1,7 +1,7 @@
 """Regenerate the golden fixtures from the reference GraviDy CPU path.
 
-Run in a checkout that has the reference sources (default
-/root/reference/src; override with GRAVIDY_REF):
+Run where the reference sources are present (the location named by REF in
+oracle/Makefile; override with GRAVIDY_REF):
 
     python tests/golden/make_golden.py
 
@@ -42,8 +42,9 @@ CASES = {
 
 
 def main() -> None:
-    ref = os.environ.get("GRAVIDY_REF", "/root/reference/src")
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={ref}"], check=True)
+    ref = os.environ.get("GRAVIDY_REF")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"] + ([f"REF={ref}"] if ref else []),
+                   check=True)
     harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
     cli = os.path.join(ROOT, "oracle", "_ref", "gravidy_ref")
     env = dict(os.environ, OMP_NUM_THREADS="1")

@@ -7,7 +7,9 @@ instead of reading or writing out of bounds.  tests/bounds_scenarios.py runs
 single systems in every force form and kernel shape, the allocation-free
 entry point, diagnostics and ensembles at N = 1, 2, 31, 33, 257, 513, 1000,
 1500, 2500 under both builds, in child processes; the checked build must report
-no violation and give bit-identical results to the normal one.
+no violation and give bit-identical results to the normal one.  The checked
+build also runs one failing allocation-free call (an active list naming a
+particle past n, which its checks refuse) and then a good one.
 """
 import json
 import os
@@ -40,3 +42,5 @@ def test_bounds_checked_build_clean_and_identical():
     diff = {k: (normal["results"][k], checked["results"][k]) for k in normal["results"]
             if normal["results"][k] != checked["results"][k]}
     assert not diff, diff
+    # a failed allocation-free call leaves no error behind for the next call
+    assert checked["checked_only"] == {"noalloc_recovers": True}

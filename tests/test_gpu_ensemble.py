@@ -144,6 +144,28 @@ def test_ensemble_mixed_forces_vs_oracle():
         assert np.median(ej) < 1e-6 and ej.max() < 1e-3, (c, np.median(ej), ej.max())
 
 
+def test_ensemble_mixed_forces_large_system_vs_oracle():
+    """An ensemble holding a 16384-particle system (the top of C4's size
+    range) beside smaller ones: initial forces (all particles active, so the
+    large systems run as block-tiled items and the small one as warp items)
+    on a sample of particles of every system against the oracle."""
+    from h4_util import rel_err_vec
+    systems = _systems([16384, 3000, 700], seed0=1500)
+    with Ensemble(systems, mode="mixed") as E:
+        E.init()
+        f = E.download()["f"]
+    for c, (m, p, v, soft, eta) in enumerate(systems):
+        sample = np.unique(np.linspace(0, len(m) - 1, min(len(m), 1024)).astype(np.uint32))
+        want = orc.forces_for(orc.make_predictors(m, p, v), orc.e2_from_softening(soft), sample)
+        got = f[E.system_slice(c)][sample]
+        ea = rel_err_vec(got[:, :3], want[:, :3])
+        ej = rel_err_vec(got[:, 3:], want[:, 3:])
+        print(f"N={len(m)}: acc median {np.median(ea):.2e} max {ea.max():.2e}; "
+              f"jerk median {np.median(ej):.2e} max {ej.max():.2e}")
+        assert np.median(ea) < 1e-6 and ea.max() < 1e-4, (c, np.median(ea), ea.max())
+        assert np.median(ej) < 1e-6 and ej.max() < 1e-3, (c, np.median(ej), ej.max())
+
+
 def test_ensemble_phase_timers():
     """Device time per phase of the persistent kernel (h4_ens_phase_times):
     every phase ran, and the phases add up to no more than the advance's

@@ -129,3 +129,23 @@ def test_switch_to_mixed_packs_current_predictors():
     # the active particles' new forces (the others keep their initial forces,
     # FP64 in a and mixed in b)
     assert np.array_equal(sa["f"][act], sb["f"][act])
+
+
+def test_mixed_salpeter_n16384_energy_error_within_2x_fp64():
+    """The C3 configuration (Salpeter-IMF Plummer, softening 0.01, eta 0.01)
+    at a quarter of its size and time: N = 16384 to t = 0.25 through the
+    device-resident block-timestep loop in both forms; the mixed form's
+    |dE/E| is within 2x of the FP64 form's."""
+    res = {}
+    for mode in ("fp64", "mixed"):
+        ns = plummer_system(16384, seed=3, imf="salpeter")
+        with Hermite4GPU(ns, mode=mode) as g:
+            g.init_acc_jrk()
+            atime = g.init_dt()
+            e0 = g.get_energy_gpu()
+            itime, atime, steps, _, _, _ = g.advance(0.25, 1e30, atime)
+            e1 = g.get_energy_gpu()
+        assert itime >= 0.25 and steps > 0
+        res[mode] = abs((e1 - e0) / e0)
+    print("N=16384 Salpeter, t=0.25, |dE/E|:", res)
+    assert res["mixed"] <= 2.0 * res["fp64"]

@@ -64,3 +64,9 @@ def test_forces_noalloc_rejects_oversize_active_set():
                              C.c_void_p(4), C.c_void_p(8), None)
     assert st == 1  # H4_ERR_ARG, before any device work
     assert "H4_NOALLOC_MAX_NACT" in L.h4_forces_noalloc_error().decode()
+    # more particles than h4_create accepts (a count that does not fit an int
+    # in the kernels): refused before any device work as well
+    st = L.h4_forces_noalloc((1 << 28) + 1, 1e-4, C.c_void_p(32), C.c_void_p(64), 5,
+                             C.c_void_p(4), C.c_void_p(8), None)
+    assert st == 1
+    assert "2^28" in L.h4_forces_noalloc_error().decode()
