@@ -33,6 +33,7 @@ SIGNATURES = {
     "h4_set_dt_limits": (_i, [_vp, _d, _d]),
     "h4_set_force_mode": (_i, [_vp, _i]),
     "h4_set_mixed_threshold": (_i, [_vp, _u]),
+    "h4_set_step_loop": (_i, [_vp, _u]),
     "h4_init_acc_jrk": (_i, [_vp]),
     "h4_init_dt": (_i, [_vp, _pd, _f, _d]),
     "h4_find_particles_to_move": (_i, [_vp, _d, _pu]),
@@ -64,14 +65,15 @@ SIGNATURES = {
     "h4_ens_create": (_i, [C.POINTER(_vp), _u, _vp, _vp, _vp, _vp, _vp, _i]),
     "h4_ens_destroy": (_i, [_vp]),
     "h4_ens_set_stream": (_i, [_vp, _vp]),
-    "h4_ens_set_tuning": (_i, [_vp, _vp, _vp]),
+    "h4_ens_set_tuning": (_i, [_vp, _vp, _vp, _vp]),
     "h4_ens_set_dt_limits": (_i, [_vp, _d, _d]),
     "h4_ens_init": (_i, [_vp]),
     "h4_ens_advance": (_i, [_vp, _vp, _pd]),
     "h4_ens_energy": (_i, [_vp, _vp, _vp]),
     "h4_ens_download": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "h4_ens_system_stats": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
-    "h4_ens_tune_force": (_i, [_vp, _u, _u, _u, C.POINTER(_f)]),
+    "h4_ens_tune_force": (_i, [_vp, _u, _u, _u, _u, C.POINTER(_f)]),
+    "h4_ens_bucket_stats": (_i, [_vp, _vp, _vp]),
     "h4_ens_timings": (_i, [_vp, C.POINTER(_f), C.POINTER(C.c_ulonglong)]),
     "h4_ens_phase_times": (_i, [_vp, _vp]),
     "h4_forces_noalloc_error": (C.c_char_p, []),

@@ -1,11 +1,29 @@
-"""Autotuner of the ensemble force phase: particles per warp item (1, 2, 4)
-and j-chunk length, per (N bucket, N_act bucket).
+"""Autotuner of the ensemble force phase, per (N bucket, N_act bucket).
 
-For every bucket it builds a homogeneous ensemble (about 2^20 particles in
-systems of the bucket's N), forces the bucket's active count on every system,
-times the force phase alone (h4_ens_tune_force, CUDA events) for each
-candidate, and keeps the fastest.  The table is written as JSON, one table per
-force mode, and read by ``gravidy_gb300.ensemble.Ensemble``.
+Tuned shape of a system's force work (include/gravidy_gb300.h, the tuning
+table of h4_ens_set_tuning):
+  * FP64 form: particles per warp item (1, 2, 4) x j-chunk length;
+  * mixed form: warp items of 1 particle or a packed pair (lanes over j) x
+    j-chunk length, or block-tiled items of 16 ... 512 particles (lanes over
+    i, j tiles in shared memory) x j-chunk length x shared-memory j tile
+    (128 or 256).
+
+The tuning follows the workload's mixture.  First the C4 ensemble (256
+Plummer systems, N log-uniform in [512, 16384], half equal-mass, half
+Salpeter) is integrated for a short time with the default table (to t = 0.25
+mixed, 0.0625 FP64), and the
+library's per-bucket statistics (h4_ens_bucket_stats: block steps and
+interactions per bucket) give each bucket's weight and its typical active
+count (interaction-weighted mean).  Then, for every bucket, a homogeneous
+ensemble of that bucket's N (about 2^20 particles, equal-mass and Salpeter
+systems alternating) is timed with that active count forced on every system
+(h4_ens_tune_force: the force phase, CUDA events) for every candidate shape.
+The fastest candidate wins, with a deterministic tie rule so that a re-run
+reproduces the table: among the candidates within TIE of the fastest, the one
+first in CANDIDATE order.  Buckets that C4 never reaches are tuned at a
+representative active count.  Finally the C4 ensemble is run (to t = 1
+mixed, 0.125 FP64) with the default and with the tuned table and both device
+times are recorded.
 
     python -m gravidy_gb300.autotune --out gravidy_gb300/tuning/ensemble_gb300.json
 """
@@ -17,57 +35,139 @@ import time
 
 import numpy as np
 
-from . import ics
+from . import ics, workloads
 from .ensemble import NB_A, NB_N, Ensemble
 
 N_REP = [512, 1024, 2048, 4096, 8192, 16384]
-A_REP = [1, 3, 12, 48, 192, 768, 3072, 8192]      # one count inside each active bucket
-IG_CAND = [1, 2, 4]
-CHUNK_CAND = [64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384]
+A_LO = [1, 2, 4, 16, 64, 256, 1024, 4096]          # first active count of each bucket
+A_REP = [1, 3, 12, 48, 192, 768, 3072, 8192]       # count used where C4 gives none
+TIE = 0.04
+CHUNKS = [64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384]
+
+
+def candidates(mode: str, n: int, nact: int):
+    """(ig, chunk, jtile) candidates in preference order (ties go to the
+    first): fewer, larger items first."""
+    out = []
+    if mode == "mixed":
+        for bti in (512, 256, 128, 64, 32, 16):
+            if bti > 2 * max(nact, 8):
+                continue
+            for chunk in (8192, 4096, 2048, 1024, 512):
+                if chunk > 2 * n:
+                    continue
+                for jt in (256, 128):
+                    out.append((bti, chunk, jt))
+        for ig in (2, 1):
+            for chunk in reversed(CHUNKS):
+                if chunk <= 2 * n:
+                    out.append((ig, chunk, 256))
+    else:
+        for ig in (4, 2, 1):
+            for chunk in reversed(CHUNKS):
+                if chunk <= 2 * n:
+                    out.append((ig, chunk, 256))
+    return out
+
+
+def record_mixture(mode: str, t_end: float = 0.25, verbose: bool = True):
+    """Block steps and interactions per bucket of the C4 ensemble run to
+    t_end with the default table."""
+    systems = workloads.c4_systems(256, seed=4)
+    with Ensemble(systems, mode=mode, tuning=None) as E:
+        E.init()
+        E.advance(t_end)
+        steps, inter = E.bucket_stats()
+    if verbose:
+        print(f"{mode}: C4 mixture to t={t_end}: {int(steps.sum())} block steps, {float(inter.sum()):.3e} "
+              f"interactions", flush=True)
+    return steps.astype(np.float64), inter.astype(np.float64)
+
+
+def probe_ensemble(mode: str, n: int, total_particles: int):
+    k = max(1, min(256, total_particles // n))
+    systems = []
+    for s in range(k):
+        m, p, v = ics.plummer(n, 10_000 + s, "equal" if s % 2 == 0 else "salpeter", exact_scaling_max_n=0)
+        systems.append((m, p, v, 0.01, 0.01))
+    return Ensemble(systems, mode=mode, tuning=None), k
+
+
+def time_candidate(E, nact, cand, reps):
+    ig, chunk, jt = cand
+    t = E.tune_force(nact, ig, chunk, jt)
+    if t < 50.0:   # repeat the short probes, keep the best
+        t = min([t] + [E.tune_force(nact, ig, chunk, jt) for _ in range(reps - 1)])
+    return t
+
+
+# C4 run lengths: the mixture record and the validation (the FP64 form runs
+# about 22x longer than the mixed form, so it records and validates shorter)
+RECORD_T = {"mixed": 0.25, "fp64": 0.0625}
+VALIDATE_T = {"mixed": 1.0, "fp64": 0.125}
 
 
 def tune(mode: str, total_particles: int = 1 << 20, reps: int = 3, verbose: bool = True) -> dict:
-    ig_tab = np.full((NB_N, NB_A), 4, dtype=int)
-    ch_tab = np.full((NB_N, NB_A), 1024, dtype=int)
+    steps, inter = record_mixture(mode, t_end=RECORD_T[mode], verbose=verbose)
+    ig_tab = np.zeros((NB_N, NB_A), dtype=int)
+    ch_tab = np.zeros((NB_N, NB_A), dtype=int)
+    jt_tab = np.full((NB_N, NB_A), 256, dtype=int)
     rate_tab = np.zeros((NB_N, NB_A))
+    nact_tab = np.zeros((NB_N, NB_A), dtype=int)
     for b, n in enumerate(N_REP):
-        k = max(1, min(256, total_particles // n))
-        systems = []
-        for s in range(k):
-            m, p, v = ics.plummer(n, 10_000 + s, "equal", exact_scaling_max_n=0)
-            systems.append((m, p, v, 0.01, 0.01))
-        with Ensemble(systems, mode=mode, tuning=None) as E:
-            for a, nact in enumerate(A_REP):
-                nact = min(nact, n)
-                best = None
-                for ig in IG_CAND:
-                    for chunk in CHUNK_CAND:
-                        if chunk > 2 * n:
-                            continue
-                        t = E.tune_force(nact, ig, chunk)
-                        if t < 50.0:   # repeat the short probes, keep the best
-                            t = min([t] + [E.tune_force(nact, ig, chunk) for _ in range(reps - 1)])
-                        if best is None or t < best[0]:
-                            best = (t, ig, chunk)
-                t, ig, chunk = best
-                ig_tab[b, a], ch_tab[b, a] = ig, chunk
-                rate_tab[b, a] = k * nact * n / (t * 1e-3)
+        E, k = probe_ensemble(mode, n, total_particles)
+        with E:
+            for a in range(NB_A):
+                if steps[b, a] > 0:   # interaction-weighted mean active count of the bucket
+                    nact = int(round(inter[b, a] / steps[b, a] / n))
+                    nact = max(A_LO[a], min(nact, (A_LO[a + 1] - 1) if a + 1 < NB_A else nact))
+                else:
+                    nact = A_REP[a]
+                nact = max(1, min(nact, n))
+                nact_tab[b, a] = nact
+                cands = candidates(mode, n, nact)
+                times = [time_candidate(E, nact, c, reps) for c in cands]
+                best = min(times)
+                pick = next(i for i, t in enumerate(times) if t <= best * (1.0 + TIE))
+                ig, chunk, jt = cands[pick]
+                ig_tab[b, a], ch_tab[b, a], jt_tab[b, a] = ig, chunk, jt
+                rate_tab[b, a] = k * nact * n / (times[pick] * 1e-3)
                 if verbose:
-                    print(f"{mode} N={n:6d} nact={nact:6d} systems={k:4d}: ig={ig} chunk={chunk:6d} "
-                          f"{t:8.4f} ms {rate_tab[b, a]:.3e} int/s", flush=True)
-    return {"ig": ig_tab.tolist(), "chunk": ch_tab.tolist(), "interactions_per_s": rate_tab.tolist(),
-            "n_rep": N_REP, "nact_rep": A_REP}
+                    print(f"{mode} N={n:6d} nact={nact:6d} systems={k:4d} weight={inter[b, a]:.2e}: ig={ig} "
+                          f"chunk={chunk:6d} jtile={jt} {times[pick]:8.4f} ms (best {best:8.4f}) "
+                          f"{rate_tab[b, a]:.3e} int/s", flush=True)
+    table = {"ig": ig_tab.tolist(), "chunk": ch_tab.tolist(), "jtile": jt_tab.tolist(),
+             "interactions_per_s": rate_tab.tolist(), "n_rep": N_REP, "nact_probe": nact_tab.tolist(),
+             "c4_steps": steps.astype(int).tolist(), "c4_interactions": inter.tolist()}
+    return table
+
+
+def validate_c4(mode: str, table: dict, t_end: float = 1.0) -> dict:
+    """C4 to t_end with the default table and with `table`: device seconds."""
+    systems = workloads.c4_systems(256, seed=4)
+    out = {}
+    for name, tuning in (("default", None), ("tuned", table)):
+        with Ensemble(systems, mode=mode, tuning=tuning) as E:
+            E.init()
+            st = E.advance(t_end)
+            ms, _ = E.timings()
+        out[name] = {"device_seconds": ms * 1e-3, "interactions_per_s": st["interactions"] / (ms * 1e-3)}
+    return out
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--modes", default="fp64,mixed")
+    ap.add_argument("--no-validate", action="store_true")
     args = ap.parse_args()
     t0 = time.time()
     out = {"generated_by": "python -m gravidy_gb300.autotune", "modes": {}}
     for mode in args.modes.split(","):
         out["modes"][mode] = tune(mode)
+        if not args.no_validate:
+            out["modes"][mode]["c4_validation"] = validate_c4(mode, out["modes"][mode], VALIDATE_T[mode])
+            print(mode, "C4 validation:", out["modes"][mode]["c4_validation"], flush=True)
     out["seconds"] = time.time() - t0
     with open(args.out, "w") as fh:
         json.dump(out, fh, indent=1)

@@ -9,13 +9,14 @@
 // barriers:
 //   A  per system (one block): next block time (min t + dt), the reference's
 //      loop condition, ordered active set, force work layout for its
-//      (N, N_act): warp items from the tuning table, or block-tiled items
-//      (mixed form, N_act >= BLOCK_MIN_NACT);
+//      (N, N_act) from the tuning table: warp items (lanes over j), or in the
+//      mixed form block-tiled items (lanes over i, j tiles in shared memory);
 //   B  all threads: predictor of every particle of the stepping systems;
-//   C  all blocks: the force sums -- block-tiled items (shared-memory j tiles,
-//      packed f32x2) then warp items, each from one global work queue (the
-//      systems' item counts are prefix-summed in shared memory, an item finds
-//      its system by binary search);
+//   C  all blocks: the force sums -- block-tiled items (j tiles brought into
+//      shared memory by TMA bulk copies on an mbarrier, double buffered;
+//      packed f32x2) then warp items, each kind from one global work queue
+//      (the systems' item counts are prefix-summed in shared memory, an item
+//      finds its system by binary search);
 //   D  all threads: fixed-order reduction of the partial forces, save of the
 //      old forces, corrector and new timestep of every active particle.
 // The O(N) and O(N_act) phases are spread over the whole GPU: FP64
@@ -37,14 +38,20 @@
 #include "h4_exact.cuh"
 #include "h4_internal.cuh"
 #include "h4_pair.cuh"
+#include "h4_tma.cuh"
 
 namespace h4 {
 namespace ens {
 
-// Resident blocks per SM the register allocation must allow (build knob).
-#ifndef H4_ENS_MIN_BLOCKS
-#define H4_ENS_MIN_BLOCKS 1
+// Resident blocks per SM the register allocation must allow: two in the
+// mixed form (16 warps per SM for the FP32 force items; every phase fits 128
+// registers a thread), one in the FP64 and exact forms (their FP64 warp items
+// need more registers).  Build knob for the mixed form.
+#ifndef H4_ENS_MIN_BLOCKS_MIXED
+#define H4_ENS_MIN_BLOCKS_MIXED 2
 #endif
+template <int MODE>
+constexpr int kMinBlocks = MODE == H4_FORCE_MIXED ? H4_ENS_MIN_BLOCKS_MIXED : 1;
 constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
 constexpr int NB_N = H4_ENS_TUNE_NB_N;
@@ -52,22 +59,27 @@ constexpr int NB_A = H4_ENS_TUNE_NB_A;
 constexpr unsigned long long BARRIER_TIMEOUT_NS = 60ull * 1000000000ull;
 constexpr int ITERS_PER_LAUNCH = 16;
 constexpr unsigned MAX_SYSTEMS = 4096;
-#ifndef H4_ENS_BLOCK_MIN_NACT
-#define H4_ENS_BLOCK_MIN_NACT 2048
-#endif
-constexpr unsigned BLOCK_MIN_NACT = H4_ENS_BLOCK_MIN_NACT;   // mixed form: block-tiled items from this N_act
-constexpr int BTI = 2 * THREADS;           // active particles per block item (one packed pair per thread)
-constexpr int BJT = 256;                   // j per shared-memory tile of a block item
-constexpr int BCHUNK = 2048;               // j per block item
+// Block-tiled items (mixed form): BTI active particles (BTI / 2 packed pairs)
+// x one j-chunk, the chunk streamed through shared memory in tiles of JT j,
+// JT in {128, 256} (one instantiation each).  The block's 256 threads are
+// P = BTI / 2 pairs x Q = 256 / P j-lanes: thread (p, q) takes tile entries
+// q, q + Q, ...; each j-lane's sum is a partial of its own (partial index
+// s * Q + q), so no reduction inside the block.
+constexpr int JT_MAX = 256;
+constexpr unsigned BTI_MIN = 16, BTI_MAX = 2 * THREADS;
+constexpr unsigned WAIT_LIMIT = 1u << 26;  // mbarrier polls before a tile wait gives up
 
 struct System {
     int off, n;                  // particle offset and count
+    int joff, npad;              // offset and length (n rounded up to JT_MAX) of its block-item j data
     double e2, eta, dt_min, dt_max;
     double t_end;
     double itime, atime;         // last block time, next block time
     unsigned nact;
     unsigned ig, chunk, split, n_groups, items;
-    unsigned bitems;             // block-tiled force items (mixed form, large N_act)
+    // block-tiled items (mixed form): count, j tile, j-lanes, j-chunks
+    // (split = bsplit * q partials per particle)
+    unsigned bitems, jt, q, bsplit;
     unsigned done, err;
     size_t part_off, part_cap;   // partial-force area (doubles)
     unsigned long long steps, psteps, inter;
@@ -79,7 +91,9 @@ struct Dev {
     dbl4 *r, *v, *pr, *pv;
     double *f, *old, *a2, *a3, *t, *dt;
     float4 *jf0, *jf1, *jf2;
-    float4 *jd;                  // [5][total] duplicated j data of the block-tiled items
+    float4 *jd;                  // [5][jtotal] duplicated j data of the block-tiled items, each system's
+                                 // at joff, padded to npad with zero-mass far-away particles
+    int jtotal;
     unsigned *move;
     double *part;
     unsigned *queue;             // force work-queue head (warp items)
@@ -87,7 +101,8 @@ struct Dev {
     unsigned *bar_count, *bar_gen;
     unsigned *err;               // [2]: global error bits, first failing bounds-check site
     size_t part_total;           // doubles in part
-    unsigned *tune_ig, *tune_chunk;   // [NB_N * NB_A]
+    unsigned *tune_ig, *tune_chunk, *tune_jt;   // [NB_N * NB_A]
+    unsigned long long *bucket;  // [NB_N * NB_A][2]: block steps, interactions per (N, N_act) bucket
     unsigned *forced_nact;       // tuning probe: active count forced on every system (0 = off)
     unsigned long long *launches;     // persistent-kernel launches so far
     unsigned long long *phase_ns;     // [4] device time of phases A, B, C, D since creation
@@ -268,46 +283,71 @@ __device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *re
             S.inter += (unsigned long long)nact * (unsigned long long)n;
         }
         S.nact = nact;
-        unsigned ig, chunk, split;
+        unsigned ig, chunk, split, jt = JT_MAX, q = 1, bsplit = 0;
+        bool block = false;
         if (MODE == H4_FORCE_EXACT) {
             ig = 32; chunk = (unsigned)n; split = 1;
         } else {
             const int t = n_bucket(n) * NB_A + a_bucket(nact);
+            if (!init && !forced) {
+                atomicAdd(&d.bucket[2 * t], 1ull);
+                atomicAdd(&d.bucket[2 * t + 1], (unsigned long long)nact * (unsigned long long)n);
+            }
             ig = d.tune_ig[t];
             chunk = d.tune_chunk[t];
-            if (ig != 1 && ig != 2 && ig != 4) ig = 4;
-            chunk = max(32u, (chunk + 31u) & ~31u);
-            split = ((unsigned)n + chunk - 1) / chunk;
-            const unsigned cap = nact ? (unsigned)(S.part_cap / (6ull * nact)) : 1u;
-            if (split > cap) {
-                split = max(1u, cap);
-                chunk = (((unsigned)n + split - 1) / split + 31u) & ~31u;
+            if (MODE == H4_FORCE_MIXED && S.e2 > 0.0 && ig >= BTI_MIN && ig <= BTI_MAX && (ig & (ig - 1)) == 0) {
+                // block-tiled items of ig active particles; the j-chunk is a
+                // whole number of tiles; the partials (bsplit * q per
+                // particle) must fit the system's area, else wider items
+                // (fewer j-lanes)
+                block = true;
+                jt = d.tune_jt[t] == 128u ? 128u : (unsigned)JT_MAX;
+                chunk = max(jt, (chunk + jt - 1) / jt * jt);
+                const unsigned npad = (unsigned)S.npad;
+                for (;;) {
+                    q = (unsigned)THREADS / (ig / 2);
+                    bsplit = (npad + chunk - 1) / chunk;
+                    const unsigned cap = nact ? (unsigned)(S.part_cap / (6ull * nact * q)) : 1u;
+                    if (cap >= 1u || ig >= BTI_MAX) {
+                        if (bsplit > cap) {
+                            bsplit = max(1u, cap);
+                            chunk = ((npad + bsplit - 1) / bsplit + jt - 1) / jt * jt;
+                            bsplit = (npad + chunk - 1) / chunk;
+                        }
+                        break;
+                    }
+                    ig *= 2;
+                }
+                split = bsplit * q;
+            } else {
+                // warp items: 1, 2 or 4 particles (FP64); 1 or 2 (mixed: a
+                // packed pair)
+                if (MODE == H4_FORCE_MIXED)
+                    ig = ig == 1u ? 1u : 2u;
+                else if (ig != 1 && ig != 2 && ig != 4)
+                    ig = 4;
+                chunk = max(32u, (chunk + 31u) & ~31u);
                 split = ((unsigned)n + chunk - 1) / chunk;
+                const unsigned cap = nact ? (unsigned)(S.part_cap / (6ull * nact)) : 1u;
+                if (split > cap) {
+                    split = max(1u, cap);
+                    chunk = (((unsigned)n + split - 1) / split + 31u) & ~31u;
+                    split = ((unsigned)n + chunk - 1) / chunk;
+                }
             }
-        }
-        S.bitems = 0;
-        if (MODE == H4_FORCE_MIXED && S.e2 > 0.0 && nact >= BLOCK_MIN_NACT) {
-            // block-tiled items: 512 active particles x BCHUNK j each
-            unsigned bsplit = ((unsigned)n + BCHUNK - 1) / BCHUNK;
-            const unsigned cap = (unsigned)(S.part_cap / (6ull * nact));
-            unsigned bchunk = BCHUNK;
-            if (bsplit > cap) {
-                bsplit = max(1u, cap);
-                bchunk = ((((unsigned)n + bsplit - 1) / bsplit) + BJT - 1) / BJT * BJT;
-                bsplit = ((unsigned)n + bchunk - 1) / bchunk;
-            }
-            ig = BTI;
-            chunk = bchunk;
-            split = bsplit;
         }
         S.ig = ig;
         S.chunk = chunk;
         S.split = split;
+        S.jt = jt;
+        S.q = q;
+        S.bsplit = bsplit;
         S.n_groups = nact ? (nact + ig - 1) / ig : 0;
-        if (ig == (unsigned)BTI && MODE == H4_FORCE_MIXED) {
-            S.bitems = S.n_groups * split;
+        if (block) {
+            S.bitems = S.n_groups * bsplit;
             S.items = 0;
         } else {
+            S.bitems = 0;
             S.items = S.n_groups * split;
         }
     }
@@ -356,12 +396,12 @@ __device__ __forceinline__ void predict_one(const Dev &d, const System &S, size_
         d.jf0[g] = a;
         d.jf1[g] = b;
         d.jf2[g] = cc;
-        const size_t tp = (size_t)d.total;
-        d.jd[g] = make_float4(a.x, a.x, a.y, a.y);
-        d.jd[tp + g] = make_float4(a.z, a.z, a.w, a.w);
-        d.jd[2 * tp + g] = make_float4(b.x, b.x, b.y, b.y);
-        d.jd[3 * tp + g] = make_float4(b.z, b.z, cc.x, cc.x);
-        d.jd[4 * tp + g] = make_float4(cc.y, cc.y, cc.z, cc.z);
+        const size_t tp = (size_t)d.jtotal, gj = (size_t)S.joff + (g - (size_t)S.off);
+        d.jd[gj] = make_float4(a.x, a.x, a.y, a.y);
+        d.jd[tp + gj] = make_float4(a.z, a.z, a.w, a.w);
+        d.jd[2 * tp + gj] = make_float4(b.x, b.x, b.y, b.y);
+        d.jd[3 * tp + gj] = make_float4(b.z, b.z, cc.x, cc.x);
+        d.jd[4 * tp + gj] = make_float4(cc.y, cc.y, cc.z, cc.z);
     }
 }
 
@@ -413,14 +453,11 @@ __device__ void force_item(const Dev &d, const System &S, unsigned local, int la
     } else {
         const float4 *a = d.jf0 + off, *b = d.jf1 + off, *c = d.jf2 + off;
         const float e2 = (float)S.e2;
-        if (S.e2 > 0.0) {
-            if (cnt == 4) {
-                pair::mixed_warp_item<4, false>(a, b, c, move, nact, k0, jb, je, e2, part_s, lane);
-            } else {
-                unsigned k = k0;
-                if (cnt >= 2) { pair::mixed_warp_item<2, false>(a, b, c, move, nact, k, jb, je, e2, part_s, lane); k += 2; }
-                if (cnt & 1) pair::mixed_warp_item<1, false>(a, b, c, move, nact, k, jb, je, e2, part_s, lane);
-            }
+        if (S.e2 > 0.0) {   // a packed pair, or one particle
+            if (cnt == 2)
+                pair::mixed_warp_item_x2(a, b, c, move, nact, k0, jb, je, e2, part_s, lane);
+            else
+                pair::mixed_warp_item<1, false>(a, b, c, move, nact, k0, jb, je, e2, part_s, lane);
         } else {
             unsigned k = k0;
             while (k < k0 + cnt) {
@@ -431,79 +468,107 @@ __device__ void force_item(const Dev &d, const System &S, unsigned local, int la
     }
 }
 
-// ---- P1 (mixed form, large active sets): one block item ---------------------
-// 512 active particles (a packed pair per thread) against a j-chunk that
-// streams through shared memory in tiles of 256; j past the system's end are
-// zero-mass padding (exact zero terms).  Needs e2 > 0 (the self term is then
-// an exact zero).  Sums as k_force_mixed_tiled_x2: FP32 over 64 j, Kahan
-// across, stored as doubles.
-__device__ void block_item(const Dev &d, const System &S, unsigned local, float4 (*sj)[BJT]) {
+// ---- P1 (mixed form): one block-tiled item --------------------------------------
+// S.ig active particles (P = S.ig / 2 packed pairs, one per thread of each of
+// the Q = S.q j-lanes) against one j-chunk of the system's padded j data; the
+// chunk streams through shared memory in tiles of JT j, each tile brought in
+// by five 1-D bulk copies (TMA, one per plane of the duplicated j data) that
+// complete on an mbarrier, double buffered across the block's items.  j past
+// the system's end are zero-mass padding (exact zero terms); needs e2 > 0
+// (the self term is then an exact zero).  Sums as k_force_mixed_tiled_x2:
+// FP32 over runs of at most 64 j per thread, Kahan across runs, stored as
+// doubles, j-lane q of chunk s as partial s * Q + q.  gt counts the tiles
+// this block has consumed (buffer gt & 1, parity (gt >> 1) & 1).  Returns
+// false when a tile wait timed out (the error bit is then set).
+template <int JT>
+__device__ bool block_item(const Dev &d, const System &S, unsigned local, float4 (*sj)[5][JT_MAX], uint64_t *full,
+                           unsigned &gt) {
     using namespace pair;
     const unsigned s = local / S.n_groups;
     const unsigned g = local - s * S.n_groups;
-    const int off = S.off, n = S.n;
-    const unsigned nact = S.nact;
+    const unsigned nact = S.nact, P = S.ig / 2, Q = S.q;
+    const unsigned p = threadIdx.x & (P - 1), qq = threadIdx.x / P;
     const int jb = (int)(s * S.chunk);
-    const int je = min(n, jb + (int)S.chunk);
-    const unsigned k0 = g * BTI + threadIdx.x, k1 = k0 + THREADS;
-    const unsigned *move = d.move + off;
+    const int je = min(S.npad, jb + (int)S.chunk);
+    const int ntiles = (je - jb) / JT;
+    const unsigned kb = g * S.ig, k0 = kb + p, k1 = k0 + P;
+    const unsigned *move = d.move + S.off;
     if (kBoundsCheck) {   // block-uniform ranges, then this thread's two particle indices
-        const unsigned kb = g * BTI, cnt = min((unsigned)BTI, nact - kb);
-        if (!__syncthreads_and(item_ok(d, S, s, kb, cnt, jb, je, THREADS) &&
-                               in_range(d, BS_ENS_ITEM, (long long)off + jb, (long long)off + je, d.total)))
-            return;
-        if (!__syncthreads_and(in_range(d, BS_MOVE, move[k0 < nact ? k0 : nact - 1], move[k0 < nact ? k0 : nact - 1] + 1ll, n) &&
-                               in_range(d, BS_MOVE, move[k1 < nact ? k1 : nact - 1], move[k1 < nact ? k1 : nact - 1] + 1ll, n)))
-            return;
+        const unsigned cnt = min(S.ig, nact - kb);
+        if (!__syncthreads_and(
+                system_ok(d, S) && in_range(d, BS_ENS_ITEM, 0, nact, S.n) &&
+                in_range(d, BS_ENS_ITEM, kb, (long long)kb + cnt, nact) && in_range(d, BS_ENS_ITEM, jb, je, S.npad) &&
+                in_range(d, BS_ENS_ITEM, 0, (je - jb) % JT, 1) &&
+                in_range(d, BS_ENS_ITEM, (long long)S.joff + jb, (long long)S.joff + je, d.jtotal) &&
+                in_range(d, BS_ENS_PART, 6ll * nact * s * Q, 6ll * nact * (s + 1) * Q, (long long)S.part_cap)))
+            return true;
+        const unsigned i0 = move[min(k0, nact - 1)], i1 = move[min(k1, nact - 1)];
+        if (!__syncthreads_and(in_range(d, BS_MOVE, i0, i0 + 1ll, S.n) && in_range(d, BS_MOVE, i1, i1 + 1ll, S.n)))
+            return true;
     }
-    const float4 *jf0 = d.jf0 + off, *jf1 = d.jf1 + off, *jf2 = d.jf2 + off;
-    const IParticle a = load_i(jf0, jf1, jf2, move[k0 < nact ? k0 : nact - 1]);
-    const IParticle b = load_i(jf0, jf1, jf2, move[k1 < nact ? k1 : nact - 1]);
-    IPair ip;
-    ip.xh = pk2(a.xh, b.xh); ip.yh = pk2(a.yh, b.yh); ip.zh = pk2(a.zh, b.zh);
-    ip.xl = pk2(a.xl, b.xl); ip.yl = pk2(a.yl, b.yl); ip.zl = pk2(a.zl, b.zl);
-    ip.vx = pk2(a.vx, b.vx); ip.vy = pk2(a.vy, b.vy); ip.vz = pk2(a.vz, b.vz);
+    const float4 *jf0 = d.jf0 + S.off, *jf1 = d.jf1 + S.off, *jf2 = d.jf2 + S.off;
+    const IPair ip = pack_pair(load_i(jf0, jf1, jf2, move[min(k0, nact - 1)]),
+                               load_i(jf0, jf1, jf2, move[min(k1, nact - 1)]));
     const float e2f = (float)S.e2;
     const f2 e2 = pk2(e2f, e2f), m3 = pk2(-3.0f, -3.0f);
     f2 Sum[6], Cmp[6];
 #pragma unroll
     for (int c = 0; c < 6; c++) { Sum[c] = 0ull; Cmp[c] = 0ull; }
-    const size_t tp = (size_t)d.total;
-    for (int j0 = jb; j0 < je; j0 += BJT) {
-        const int j = j0 + (int)threadIdx.x;
-        if (j < je) {
-            const size_t gj = (size_t)off + j;
+    const size_t jtp = (size_t)d.jtotal;
+    const float4 *src = d.jd + (size_t)S.joff + jb;
+    constexpr unsigned TILE_BYTES = JT * sizeof(float4);
+    if (threadIdx.x == 0) {   // the first two tiles
+        tma::fence_proxy_async();
+        for (int t = 0; t < 2 && t < ntiles; t++) {
+            const unsigned b = (gt + t) & 1u;
+            tma::mbar_arrive_expect_tx(&full[b], 5 * TILE_BYTES);
 #pragma unroll
-            for (int pl = 0; pl < 5; pl++) sj[pl][threadIdx.x] = d.jd[pl * tp + gj];
-        } else {
-            sj[0][threadIdx.x] = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 1.0e15f);
-            sj[1][threadIdx.x] = make_float4(1.0e15f, 1.0e15f, 0.f, 0.f);
-#pragma unroll
-            for (int pl = 2; pl < 5; pl++) sj[pl][threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int pl = 0; pl < 5; pl++) tma::load_1d(&sj[b][pl][0], src + pl * jtp + (size_t)t * JT, TILE_BYTES, &full[b]);
         }
-        __syncthreads();
-#pragma unroll 1
-        for (int sb = 0; sb < BJT; sb += 64) {
+    }
+    const int per = JT / (int)Q;          // j per thread per tile
+    const int sub = per > 64 ? 64 : per;  // j per FP32 run
+    for (int t = 0; t < ntiles; t++, gt++) {
+        const unsigned b = gt & 1u;
+        const bool ok = tma::wait_bounded(&full[b], (gt >> 1) & 1u, WAIT_LIMIT);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                tma::drain_tiles(full, gt, ntiles - t, WAIT_LIMIT);
+                atomicOr(d.err, (unsigned)H4_ERRBIT_TIMEOUT);
+            }
+            return false;
+        }
+        for (int sb = 0; sb < per; sb += sub) {
             f2 part[6];
 #pragma unroll
             for (int c = 0; c < 6; c++) part[c] = 0ull;
 #pragma unroll 4
-            for (int jj = sb; jj < sb + 64; jj++) {
-                const f2 *q0 = (const f2 *)&sj[0][jj], *q1 = (const f2 *)&sj[1][jj], *q2 = (const f2 *)&sj[2][jj],
-                         *q3 = (const f2 *)&sj[3][jj], *q4 = (const f2 *)&sj[4][jj];
+            for (int u = 0; u < sub; u++) {
+                const int jj = (int)qq + (sb + u) * (int)Q;
+                const f2 *q0 = (const f2 *)&sj[b][0][jj], *q1 = (const f2 *)&sj[b][1][jj],
+                         *q2 = (const f2 *)&sj[b][2][jj], *q3 = (const f2 *)&sj[b][3][jj],
+                         *q4 = (const f2 *)&sj[b][4][jj];
                 pair_x2(ip, q0[0], q0[1], q1[0], q1[1], q2[0], q2[1], q3[0], q3[1], q4[0], q4[1], e2, m3, part);
             }
 #pragma unroll
             for (int c = 0; c < 6; c++) kahan2(Sum[c], Cmp[c], part[c]);
         }
-        __syncthreads();
+        __syncthreads();   // every thread is done with buffer b
+        if (threadIdx.x == 0 && t + 2 < ntiles) {
+            tma::fence_proxy_async();
+            tma::mbar_arrive_expect_tx(&full[b], 5 * TILE_BYTES);
+#pragma unroll
+            for (int pl = 0; pl < 5; pl++)
+                tma::load_1d(&sj[b][pl][0], src + pl * jtp + (size_t)(t + 2) * JT, TILE_BYTES, &full[b]);
+        }
     }
-    double *part_s = d.part + S.part_off + (size_t)s * 6 * nact;
+    double *part_s = d.part + S.part_off + (size_t)(s * Q + qq) * 6 * nact;
 #pragma unroll
     for (int c = 0; c < 6; c++) {
         if (k0 < nact) part_s[(size_t)c * nact + k0] = (double)lo2(Sum[c]) - (double)lo2(Cmp[c]);
         if (k1 < nact) part_s[(size_t)c * nact + k1] = (double)hi2(Sum[c]) - (double)hi2(Cmp[c]);
     }
+    return true;
 }
 
 // ---- phase D (grid-wide): reduction, corrector and timestep of one active
@@ -563,7 +628,7 @@ __device__ __forceinline__ void phase_mark(const Dev &d, int phase, unsigned lon
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(THREADS, H4_ENS_MIN_BLOCKS) k_ensemble(Dev d, int iters, int init, int force_only) {
+__global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, int iters, int init, int force_only) {
     // per-system prefix sums, [nsys + 1] each: particle offsets, warp items,
     // block items, active particles
     extern __shared__ unsigned s_dyn[];
@@ -575,8 +640,19 @@ __global__ void __launch_bounds__(THREADS, H4_ENS_MIN_BLOCKS) k_ensemble(Dev d, 
     __shared__ double redd[WARPS];
     __shared__ unsigned s_item[WARPS];
     __shared__ unsigned s_bitem;
-    __shared__ __align__(16) float4 sj[MODE == H4_FORCE_MIXED ? 5 : 1][BJT];
+    // j tiles of the block items (two buffers) and their barriers
+    __shared__ __align__(128) float4 sj[MODE == H4_FORCE_MIXED ? 2 : 1][5][MODE == H4_FORCE_MIXED ? JT_MAX : 1];
+    __shared__ __align__(8) uint64_t s_full[2];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned gt = 0;   // block-item tiles consumed by this block
+    if (MODE == H4_FORCE_MIXED) {
+        if (threadIdx.x == 0) {
+            tma::mbar_init(&s_full[0], 1);
+            tma::mbar_init(&s_full[1], 1);
+            tma::mbar_init_fence();
+        }
+        __syncthreads();
+    }
     const bool from_state = init || (*d.forced_nact != 0u);
     const unsigned nthreads = gridDim.x * THREADS;
     const unsigned gtid = blockIdx.x * THREADS + threadIdx.x;
@@ -627,7 +703,8 @@ __global__ void __launch_bounds__(THREADS, H4_ENS_MIN_BLOCKS) k_ensemble(Dev d, 
         if (!grid_sync(d)) return;
         phase_mark(d, 1, t_prev);
         // C: force sums
-        if (MODE == H4_FORCE_MIXED) {
+        bool tiles_ok = true;
+        if constexpr (MODE == H4_FORCE_MIXED) {
             const unsigned total_b = c_b;
             for (;;) {
                 if (threadIdx.x == 0) s_bitem = atomicAdd(d.queue_b, 1u);
@@ -636,10 +713,13 @@ __global__ void __launch_bounds__(THREADS, H4_ENS_MIN_BLOCKS) k_ensemble(Dev d, 
                 __syncthreads();
                 if (item >= total_b) break;
                 const int c = find_seg(s_prefix_b, d.nsys, item);
-                block_item(d, d.sys[c], item - s_prefix_b[c], sj);
+                const System &S = d.sys[c];
+                tiles_ok = S.jt == 128u ? block_item<128>(d, S, item - s_prefix_b[c], sj, s_full, gt)
+                                        : block_item<JT_MAX>(d, S, item - s_prefix_b[c], sj, s_full, gt);
+                if (!tiles_ok) break;   // a tile wait timed out: straight to the barrier, which fails
             }
         }
-        const unsigned total = c_w;
+        const unsigned total = tiles_ok ? c_w : 0u;
         for (;;) {
             if (lane == 0) s_item[w] = atomicAdd(d.queue, 1u);
             __syncwarp();
@@ -694,6 +774,24 @@ __global__ void __launch_bounds__(THREADS, H4_ENS_MIN_BLOCKS) k_ensemble(Dev d, 
                 }
                 __syncthreads();
             }
+        }
+    }
+}
+
+// Padding of every system's block-item j data past its n (to npad): zero
+// mass, far away, at rest -- each such j contributes exactly zero.  Written
+// once at creation; the predictor writes only the first n entries.
+__global__ void k_ens_pad_jd(Dev d) {
+    const size_t tp = (size_t)d.jtotal;
+    for (int c = blockIdx.x; c < d.nsys; c += gridDim.x) {
+        const System &S = d.sys[c];
+        for (int i = S.n + (int)threadIdx.x; i < S.npad; i += blockDim.x) {
+            const size_t gj = (size_t)S.joff + i;
+            d.jd[gj] = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 1.0e15f);
+            d.jd[tp + gj] = make_float4(1.0e15f, 1.0e15f, 0.f, 0.f);
+            d.jd[2 * tp + gj] = make_float4(0.f, 0.f, 0.f, 0.f);
+            d.jd[3 * tp + gj] = make_float4(0.f, 0.f, 0.f, 0.f);
+            d.jd[4 * tp + gj] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
 }
@@ -881,17 +979,38 @@ void ens_free(h4_ensemble_s *E) {
     if (E->own) cudaStreamDestroy(E->own);
 }
 
-// Default tuning table: up to 4 particles per warp item; j-chunks short for
-// small active sets (more items), the whole system for large ones.
-void default_tuning(unsigned *ig, unsigned *chunk) {
+// Default tuning table (used until a tuned table is loaded).  FP64: up to 4
+// particles per warp item; j-chunks short for small active sets (more
+// items), the whole system for large ones.  Mixed: warp items of a packed
+// pair below 64 active particles, block-tiled items above (wider ones for
+// larger active sets), 2048 j per item, tiles of 256.
+void default_tuning(int mode, unsigned *ig, unsigned *chunk, unsigned *jt) {
+    static const unsigned ch[NB_A] = {128, 128, 256, 512, 1024, 2048, 4096, 8192};
+    static const unsigned mixed_ig[NB_A] = {1, 2, 2, 2, 64, 256, 512, 512};
     for (int b = 0; b < NB_N; b++) {
         for (int a = 0; a < NB_A; a++) {
             const int t = b * NB_A + a;
-            ig[t] = 4;
-            static const unsigned ch[NB_A] = {128, 128, 256, 512, 1024, 2048, 4096, 8192};
-            chunk[t] = ch[a];
+            jt[t] = JT_MAX;
+            if (mode == H4_FORCE_MIXED) {
+                ig[t] = mixed_ig[a];
+                chunk[t] = mixed_ig[a] > 2 ? 2048 : ch[a];
+            } else {
+                ig[t] = 4;
+                chunk[t] = ch[a];
+            }
         }
     }
+}
+
+// Checks a tuning table for the ensemble's force mode (see h4_ens_set_tuning).
+bool tuning_valid(int mode, const unsigned *ig, const unsigned *chunk, const unsigned *jt) {
+    for (int t = 0; t < NB_N * NB_A; t++) {
+        const bool warp = ig[t] == 1 || ig[t] == 2 || (ig[t] == 4 && mode != H4_FORCE_MIXED);
+        const bool block = mode == H4_FORCE_MIXED && ig[t] >= BTI_MIN && ig[t] <= BTI_MAX && (ig[t] & (ig[t] - 1)) == 0;
+        if (!(warp || block) || chunk[t] < 32 || chunk[t] > (1u << 24)) return false;
+        if (jt && jt[t] != 128 && jt[t] != 256) return false;
+    }
+    return true;
 }
 
 int build_ens_graph(h4_ensemble_s *E) {
@@ -969,11 +1088,14 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     d.total = (int)total;
     d.mode = mode;
     E->host_sys.resize(nsys);
-    size_t off = 0, poff = 0;
+    size_t off = 0, poff = 0, joff = 0;
     for (unsigned c = 0; c < nsys; c++) {
         System S{};
         S.off = (int)off;
         S.n = (int)n[c];
+        S.joff = (int)joff;
+        S.npad = (int)((n[c] + JT_MAX - 1) / JT_MAX * JT_MAX);
+        joff += (size_t)S.npad;
         S.e2 = e2[c];
         S.eta = (double)eta[c];
         S.dt_min = 1.1920928955078125e-07;
@@ -985,6 +1107,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
         off += n[c];
         poff += S.part_cap;
     }
+    d.jtotal = (int)joff;
     e = cudaSuccess;
 #define EA(p, cnt) if (e == cudaSuccess) e = dalloc(E, &p, cnt)
     EA(d.sys, nsys); EA(d.r, total); EA(d.v, total); EA(d.pr, total); EA(d.pv, total);
@@ -992,10 +1115,11 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     d.part_total = part_total;
     EA(d.t, total); EA(d.dt, total); EA(d.move, total); EA(d.part, part_total);
     EA(d.queue, 1); EA(d.queue_b, 1); EA(d.bar_count, 1); EA(d.bar_gen, 1); EA(d.err, 2);
-    EA(d.tune_ig, NB_N * NB_A); EA(d.tune_chunk, NB_N * NB_A); EA(d.forced_nact, 1); EA(d.launches, 1);
+    EA(d.tune_ig, NB_N * NB_A); EA(d.tune_chunk, NB_N * NB_A); EA(d.tune_jt, NB_N * NB_A);
+    EA(d.bucket, 2 * NB_N * NB_A); EA(d.forced_nact, 1); EA(d.launches, 1);
     EA(d.phase_ns, 4);
     EA(d.epot_i, total); EA(d.energy, 2 * nsys);
-    if (mode == H4_FORCE_MIXED) { EA(d.jf0, total); EA(d.jf1, total); EA(d.jf2, total); EA(d.jd, 5 * total); }
+    if (mode == H4_FORCE_MIXED) { EA(d.jf0, total); EA(d.jf1, total); EA(d.jf2, total); EA(d.jd, 5 * joff); }
 #undef EA
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->own, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&E->e0);
@@ -1005,13 +1129,19 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     cudaStream_t s = E->stream;
     std::vector<h4_double4> rr(r, r + total);
     for (auto &p : rr) p.w = (double)(float)p.w;   // masses are floats in the reference
-    std::vector<unsigned> tig(NB_N * NB_A), tch(NB_N * NB_A);
-    default_tuning(tig.data(), tch.data());
+    std::vector<unsigned> tig(NB_N * NB_A), tch(NB_N * NB_A), tjt(NB_N * NB_A);
+    default_tuning(mode, tig.data(), tch.data(), tjt.data());
     e = cudaMemcpy(d.sys, E->host_sys.data(), sizeof(System) * nsys, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d.r, rr.data(), sizeof(dbl4) * total, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d.v, v, sizeof(dbl4) * total, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d.tune_ig, tig.data(), sizeof(unsigned) * tig.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d.tune_chunk, tch.data(), sizeof(unsigned) * tch.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d.tune_jt, tjt.data(), sizeof(unsigned) * tjt.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.bucket, 0, sizeof(unsigned long long) * 2 * NB_N * NB_A, s);
+    if (e == cudaSuccess && mode == H4_FORCE_MIXED) {   // zero-mass padding of the block items' j data
+        k_ens_pad_jd<<<std::min(nsys, 4096u), THREADS, 0, s>>>(d);
+        e = cudaGetLastError();
+    }
     void *zero[] = {d.f, d.old, d.a2, d.a3, d.t, d.dt};
     size_t zb[] = {48 * total, 48 * total, 24 * total, 24 * total, 8 * total, 8 * total};
     for (int k = 0; k < 6 && e == cudaSuccess; k++) e = cudaMemsetAsync(zero[k], 0, zb[k], s);
@@ -1054,14 +1184,33 @@ int h4_ens_set_stream(h4_ens_handle E, void *stream) {
     return H4_OK;
 }
 
-int h4_ens_set_tuning(h4_ens_handle E, const unsigned int *ig, const unsigned int *chunk) {
+int h4_ens_set_tuning(h4_ens_handle E, const unsigned int *ig, const unsigned int *chunk, const unsigned int *jtile) {
     if (!E || !ig || !chunk) return efail(H4_ERR_ARG, "h4_ens_set_tuning: null argument");
-    for (int t = 0; t < NB_N * NB_A; t++)
-        if ((ig[t] != 1 && ig[t] != 2 && ig[t] != 4) || chunk[t] < 32 || chunk[t] > (1u << 24))
-            return efail(H4_ERR_ARG, "h4_ens_set_tuning: ig must be 1, 2 or 4 and chunk in [32, 2^24]");
+    if (!tuning_valid(E->mode, ig, chunk, jtile))
+        return efail(H4_ERR_ARG, E->mode == H4_FORCE_MIXED
+                                     ? "h4_ens_set_tuning: ig must be 1 or 2 (warp items) or a power of two in "
+                                       "[16, 512] (block items), chunk in [32, 2^24], jtile 128 or 256"
+                                     : "h4_ens_set_tuning: ig must be 1, 2 or 4 and chunk in [32, 2^24]");
+    std::vector<unsigned> jt(NB_N * NB_A, (unsigned)JT_MAX);
+    if (jtile) jt.assign(jtile, jtile + NB_N * NB_A);
     ENS_TRY(cudaMemcpyAsync(E->d.tune_ig, ig, sizeof(unsigned) * NB_N * NB_A, cudaMemcpyHostToDevice, E->stream), "tuning");
     ENS_TRY(cudaMemcpyAsync(E->d.tune_chunk, chunk, sizeof(unsigned) * NB_N * NB_A, cudaMemcpyHostToDevice, E->stream), "tuning");
+    ENS_TRY(cudaMemcpyAsync(E->d.tune_jt, jt.data(), sizeof(unsigned) * NB_N * NB_A, cudaMemcpyHostToDevice, E->stream),
+            "tuning");
     ENS_TRY(cudaStreamSynchronize(E->stream), "tuning");
+    return H4_OK;
+}
+
+int h4_ens_bucket_stats(h4_ens_handle E, unsigned long long *steps, unsigned long long *inter) {
+    if (!E) return efail(H4_ERR_ARG, "null handle");
+    std::vector<unsigned long long> b(2 * NB_N * NB_A);
+    ENS_TRY(cudaMemcpyAsync(b.data(), E->d.bucket, sizeof(unsigned long long) * b.size(), cudaMemcpyDeviceToHost,
+                            E->stream), "bucket statistics");
+    ENS_TRY(cudaStreamSynchronize(E->stream), "bucket statistics");
+    for (int t = 0; t < NB_N * NB_A; t++) {
+        if (steps) steps[t] = b[2 * t];
+        if (inter) inter[t] = b[2 * t + 1];
+    }
     return H4_OK;
 }
 
@@ -1193,12 +1342,12 @@ int h4_ens_system_stats(h4_ens_handle E, double *itime, double *atime, unsigned 
     return H4_OK;
 }
 
-int h4_ens_tune_force(h4_ens_handle E, unsigned int nact, unsigned int ig, unsigned int chunk, float *ms) {
+int h4_ens_tune_force(h4_ens_handle E, unsigned int nact, unsigned int ig, unsigned int chunk, unsigned int jtile,
+                      float *ms) {
     if (!E || !ms) return efail(H4_ERR_ARG, "null argument");
     if (nact < 1) return efail(H4_ERR_ARG, "nact must be >= 1");
-    if (ig != 1 && ig != 2 && ig != 4) return efail(H4_ERR_ARG, "ig must be 1, 2 or 4");
-    std::vector<unsigned> tig(NB_N * NB_A, ig), tch(NB_N * NB_A, chunk);
-    int st = h4_ens_set_tuning(E, tig.data(), tch.data());
+    std::vector<unsigned> tig(NB_N * NB_A, ig), tch(NB_N * NB_A, chunk), tjt(NB_N * NB_A, jtile ? jtile : JT_MAX);
+    int st = h4_ens_set_tuning(E, tig.data(), tch.data(), tjt.data());
     if (st) return st;
     if ((st = pull_systems(E))) return st;
     for (auto &S : E->host_sys) S.done = 0;

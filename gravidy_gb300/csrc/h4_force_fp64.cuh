@@ -1,0 +1,90 @@
+// FP64 force sum of the active particles as a device routine: shared by the
+// force kernel (h4_force_fp64.cu) and the persistent step loop
+// (h4_step_loop.cu), which must produce the same work items, and hence the
+// same summation order, from the same active set.
+#pragma once
+#include "h4_internal.cuh"
+#include "h4_pair.cuh"
+
+namespace h4 {
+namespace fp64 {
+
+#ifndef H4_FP64_IG
+#define H4_FP64_IG 4
+#endif
+#ifndef H4_FP64_BPS
+#define H4_FP64_BPS 2
+#endif
+constexpr int WARPS = 4;        // warps per block of the force kernel
+constexpr int IG = H4_FP64_IG;  // active particles per work item (build knob: 2, 4 or 8)
+constexpr int ITEMS_PER_WARP = 12;
+
+// Warp `warp` (lane `lane`) of `nwarps` takes work items from the queue in
+// the control block until it is empty.  The j-split is fixed by nact, n and
+// `split_warps` (the warp count the split is sized for: enough items for
+// every warp to take several, chunks of at least 64 j, partial sums within
+// the scratch), not by the warps that actually run, so any launch shape gives
+// the same items.  first: this caller publishes the split.
+__device__ __forceinline__ void force_items(const H4Dev &d, unsigned split_warps, int lane, bool first) {
+    const unsigned nact = d.ctrl->nact;
+    if (nact == 0) return;
+    const unsigned n_groups = (nact + IG - 1) / IG;
+    unsigned split = (split_warps * ITEMS_PER_WARP + n_groups - 1) / n_groups;
+    unsigned max_split = (unsigned)((d.n + 63) / 64);
+    if (split > max_split) split = max_split;
+    const unsigned cap_split = (unsigned)(d.part_cap / (6ull * nact));
+    if (split > cap_split) split = cap_split;
+    if (split < 1) split = 1;
+    int chunk = (d.n + (int)split - 1) / (int)split;
+    chunk = (chunk + 31) & ~31;
+    split = (unsigned)((d.n + chunk - 1) / chunk);
+    const unsigned total = n_groups * split;
+    if (first) {
+        d.ctrl->force_split = split;
+        d.ctrl->work_total = total;
+    }
+    for (;;) {
+        unsigned item;
+        if (lane == 0) item = atomicAdd(&d.ctrl->work_next, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        const unsigned s = item / n_groups;
+        const unsigned g = item - s * n_groups;
+        const int j_begin = (int)s * chunk;
+        const int j_end = min(d.n, j_begin + chunk);
+        const unsigned k0 = g * IG;
+        const unsigned cnt = min((unsigned)IG, nact - k0);
+        double *part_s = d.part + (size_t)s * 6 * nact;
+        if (kBoundsCheck && !pair::warp_item_ok(d, nact, k0, cnt, j_begin, j_end, s, lane, BS_FP64_J)) continue;
+        if (cnt == (unsigned)IG) {
+            pair::fp64_warp_item<IG>(d.pr, d.pv, d.move, nact, k0, j_begin, j_end, d.e2, part_s, lane);
+        } else {
+            unsigned k = k0, left = cnt;
+            if (IG > 4 && left >= 4) {
+                pair::fp64_warp_item<4>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
+                k += 4; left -= 4;
+            }
+            if (left >= 2) {
+                pair::fp64_warp_item<2>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
+                k += 2; left -= 2;
+            }
+            if (left & 1) pair::fp64_warp_item<1>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
+        }
+    }
+}
+
+// Bit-identical restatement of Hermite4CPU::update_acc_jrk for active
+// particle k: one thread, j in ascending order, the reference's operation
+// order with no FMA contraction, IEEE sqrt and division (S = 1).
+__device__ __forceinline__ void exact_particle(const H4Dev &d, unsigned nact, unsigned k) {
+    if (!range_ok(d, BS_NACT, 0, nact, d.n) || !range_ok(d, BS_PART, 0, 6ll * nact, (long long)d.part_cap) ||
+        !range_ok(d, BS_MOVE, d.move[k], d.move[k] + 1ll, d.n))
+        return;
+    double f[6];
+    pair::exact_sum(d.pr, d.pv, d.n, d.move[k], d.e2, f);
+#pragma unroll
+    for (int c = 0; c < 6; c++) d.part[(size_t)c * nact + k] = f[c];
+}
+
+}  // namespace fp64
+}  // namespace h4

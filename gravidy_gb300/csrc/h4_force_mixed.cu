@@ -33,6 +33,7 @@
 
 #include "h4_internal.cuh"
 #include "h4_pair.cuh"
+#include "h4_tma.cuh"
 
 namespace h4 {
 namespace {
@@ -46,53 +47,13 @@ constexpr int WARPS_W = 4;              // warps per block (warp-item shape)
 constexpr int IGW = 4;                  // active particles per warp item
 constexpr unsigned WAIT_LIMIT = 1u << 26;
 
-__device__ __forceinline__ unsigned smem_addr(const void *p) {
-    return (unsigned)__cvta_generic_to_shared(p);
-}
+using tma::smem_addr;
+using tma::mbar_arrive_expect_tx;
+using tma::mbar_init;
+using tma::mbar_try_wait;
 
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Timeout path of the double-buffered tile loop: before the block leaves,
-// wait (bounded again) for the copies it may still have in flight into its
-// shared memory -- the tile that timed out (global tile index gt) and the
-// one after it, if issued -- so that no bulk copy lands in the shared memory
-// of a block that has exited.
-__device__ __forceinline__ void drain_tiles(uint64_t *full, unsigned gt, int tiles_left) {
-    for (int k = 0; k < 2 && k < tiles_left; k++) {
-        const unsigned g = gt + (unsigned)k;
-        unsigned spins = 0;
-        while (!mbar_try_wait(&full[g & 1u], (g >> 1) & 1u) && ++spins < WAIT_LIMIT) {
-        }
-    }
-}
-
-// 1-D bulk copy global -> shared, completion counted on `bar` (16-byte
-// aligned addresses, size a multiple of 16).
 __device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(smem_addr(bar))
-        : "memory");
+    tma::load_1d(dst, src, bytes, bar);
 }
 
 using pair::IParticle;
@@ -205,7 +166,7 @@ __global__ void __launch_bounds__(MT, 3) k_force_mixed_tiled(H4Dev d, unsigned t
             }
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
-                    drain_tiles(full, gt, ntiles - t);
+                    tma::drain_tiles(full, gt, ntiles - t, WAIT_LIMIT);
                     atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_TIMEOUT);
                 }
                 return;
@@ -373,7 +334,7 @@ __global__ void __launch_bounds__(MT, H4_X2_BPS) k_force_mixed_tiled_x2(H4Dev d,
             }
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
-                    drain_tiles(full, gt, ntiles - t);
+                    tma::drain_tiles(full, gt, ntiles - t, WAIT_LIMIT);
                     atomicOr(&d.ctrl->err, (unsigned)H4_ERRBIT_TIMEOUT);
                 }
                 return;

@@ -18,12 +18,18 @@
 #ifndef H4_MIXED_JUNROLL
 #define H4_MIXED_JUNROLL 2
 #endif
+// j-loop unroll of the packed-pair mixed warp item (1: it then fits the
+// 128 registers a thread of the two-blocks-per-SM ensemble kernel has).
+#ifndef H4_MIXED_X2_JUNROLL
+#define H4_MIXED_X2_JUNROLL 1
+#endif
 
 namespace h4 {
 namespace pair {
 
 constexpr int kFp64JUnroll = H4_FP64_JUNROLL;
 constexpr int kMixedJUnroll = H4_MIXED_JUNROLL;
+constexpr int kMixedX2JUnroll = H4_MIXED_X2_JUNROLL;
 
 // 1/sqrt(x) in FP64: hardware reciprocal-square-root approximation
 // (rsqrt.approx.f64) refined by one cubic Householder step,
@@ -380,6 +386,14 @@ __device__ __forceinline__ void kahan2(f2 &s, f2 &c, f2 x) {
     s = t;
 }
 
+__device__ __forceinline__ IPair pack_pair(const IParticle &a, const IParticle &b) {
+    IPair p;
+    p.xh = pk2(a.xh, b.xh); p.yh = pk2(a.yh, b.yh); p.zh = pk2(a.zh, b.zh);
+    p.xl = pk2(a.xl, b.xl); p.yl = pk2(a.yl, b.yl); p.zl = pk2(a.zl, b.zl);
+    p.vx = pk2(a.vx, b.vx); p.vy = pk2(a.vy, b.vy); p.vz = pk2(a.vz, b.vz);
+    return p;
+}
+
 __device__ __forceinline__ void pair_x2(const IPair &p, f2 jxh, f2 jyh, f2 jzh, f2 jm, f2 jxl, f2 jyl, f2 jzl,
                                         f2 jvx, f2 jvy, f2 jvz, f2 e2, f2 m3, f2 sum[6]) {
     const f2 dx = add2(sub2(jxh, p.xh), sub2(jxl, p.xl));
@@ -398,6 +412,52 @@ __device__ __forceinline__ void pair_x2(const IPair &p, f2 jxh, f2 jyh, f2 jzh, 
     sum[3] = fma2(A, fma2(eta, dx, dvx), sum[3]);
     sum[4] = fma2(A, fma2(eta, dy, dvy), sum[4]);
     sum[5] = fma2(A, fma2(eta, dz, dvz), sum[5]);
+}
+
+// Mixed warp item of two active particles (k0, k0 + 1) held as one packed
+// f32x2 pair: the lanes take interleaved j straight from L2 as
+// mixed_warp_item does, and every FP32 operation of the pair formula is one
+// packed instruction for both particles (the j values are duplicated into
+// both halves of a register pair).  Needs e2 > 0 (the self term is then an
+// exact zero).  Same sums as mixed_warp_item: FP32 over runs of 16 j per
+// lane, Kahan across runs, double-single reduce-scatter across lanes.
+__device__ __forceinline__ void mixed_warp_item_x2(const float4 *__restrict__ jf0, const float4 *__restrict__ jf1,
+                                                   const float4 *__restrict__ jf2, const unsigned *__restrict__ move,
+                                                   unsigned nact, unsigned k0, int j_begin, int j_end, float e2f,
+                                                   double *part_s, int lane) {
+    const IPair ip = pack_pair(load_i(jf0, jf1, jf2, move[k0]), load_i(jf0, jf1, jf2, move[k0 + 1]));
+    const f2 e2 = pk2(e2f, e2f), m3 = pk2(-3.0f, -3.0f);
+    f2 S[6], Cc[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) { S[c] = 0ull; Cc[c] = 0ull; }
+    for (int jb = j_begin; jb < j_end; jb += 32 * 16) {
+        f2 part[6];
+#pragma unroll
+        for (int c = 0; c < 6; c++) part[c] = 0ull;
+        const int jl = min(j_end, jb + 32 * 16);
+#pragma unroll kMixedX2JUnroll
+        for (int j = jb + lane; j < jl; j += 32) {
+            const float4 a = jf0[j], b = jf1[j], c = jf2[j];
+            pair_x2(ip, pk2(a.x, a.x), pk2(a.y, a.y), pk2(a.z, a.z), pk2(a.w, a.w), pk2(b.x, b.x), pk2(b.y, b.y),
+                    pk2(b.z, b.z), pk2(c.x, c.x), pk2(c.y, c.y), pk2(c.z, c.z), e2, m3, part);
+        }
+#pragma unroll
+        for (int c = 0; c < 6; c++) kahan2(S[c], Cc[c], part[c]);
+    }
+    // value c * 2 + q = component c of particle q; zero padding to 16
+    float h[16], l[16];
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+        h[2 * c] = lo2(S[c]);
+        h[2 * c + 1] = hi2(S[c]);
+        l[2 * c] = -lo2(Cc[c]);
+        l[2 * c + 1] = -hi2(Cc[c]);
+    }
+#pragma unroll
+    for (int x = 12; x < 16; x++) { h[x] = 0.f; l[x] = 0.f; }
+    rs_sum_ds<16, 16>(h, l, lane);
+    const int x = rs_index<16>(lane);
+    if (rs_first<16>(lane) && x < 12) part_s[(size_t)(x >> 1) * nact + k0 + (x & 1)] = (double)h[0] + (double)l[0];
 }
 
 }  // namespace pair

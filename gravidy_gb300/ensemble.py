@@ -3,8 +3,9 @@
 Each system is integrated exactly as a single system would be by
 ``Hermite4GPU.integration`` (its own block time, active set and timesteps);
 all of them advance together in one persistent fused kernel per iteration,
-replayed from a CUDA graph.  The tuning table (particles per warp item and
-j-chunk length per (N, N_act) bucket) comes from ``gravidy_gb300.autotune``.
+replayed from a CUDA graph.  The tuning table (per (N, N_act) bucket: warp
+items of 1-2 particles or block-tiled items of 16-512 particles, the j-chunk
+length and the shared-memory j tile) comes from ``gravidy_gb300.autotune``.
 """
 from __future__ import annotations
 
@@ -74,10 +75,14 @@ class Ensemble:
             if self.mode not in tuning["modes"]:
                 return
             tuning = tuning["modes"][self.mode]
+        if self.mode == "mixed" and "jtile" not in tuning:
+            return   # a table from before the block-tiled items were tuned: keep the built-in one
         ig = np.ascontiguousarray(np.array(tuning["ig"], dtype=np.uint32).reshape(-1))
         ch = np.ascontiguousarray(np.array(tuning["chunk"], dtype=np.uint32).reshape(-1))
-        assert ig.size == NB_N * NB_A and ch.size == NB_N * NB_A
-        _lib.check_ens(self.L.h4_ens_set_tuning(self.h, ig.ctypes.data, ch.ctypes.data))
+        jt = np.ascontiguousarray(np.array(tuning.get("jtile", np.full(NB_N * NB_A, 256)),
+                                           dtype=np.uint32).reshape(-1))
+        assert ig.size == NB_N * NB_A and ch.size == NB_N * NB_A and jt.size == NB_N * NB_A
+        _lib.check_ens(self.L.h4_ens_set_tuning(self.h, ig.ctypes.data, ch.ctypes.data, jt.ctypes.data))
 
     def set_dt_limits(self, dt_min, dt_max):
         _lib.check_ens(self.L.h4_ens_set_dt_limits(self.h, dt_min, dt_max))
@@ -114,10 +119,18 @@ class Ensemble:
                                                   ps.ctypes.data, inter.ctypes.data))
         return {"itime": it, "atime": at, "steps": steps, "psteps": ps, "interactions": inter}
 
-    def tune_force(self, nact: int, ig: int, chunk: int) -> float:
+    def tune_force(self, nact: int, ig: int, chunk: int, jtile: int = 256) -> float:
         ms = C.c_float()
-        _lib.check_ens(self.L.h4_ens_tune_force(self.h, nact, ig, chunk, C.byref(ms)))
+        _lib.check_ens(self.L.h4_ens_tune_force(self.h, nact, ig, chunk, jtile, C.byref(ms)))
         return ms.value
+
+    def bucket_stats(self):
+        """Block steps and interactions per (N bucket, N_act bucket) of the
+        tuning table, since creation: arrays of shape (NB_N, NB_A)."""
+        steps = np.zeros(NB_N * NB_A, np.uint64)
+        inter = np.zeros(NB_N * NB_A, np.uint64)
+        _lib.check_ens(self.L.h4_ens_bucket_stats(self.h, steps.ctypes.data, inter.ctypes.data))
+        return steps.reshape(NB_N, NB_A), inter.reshape(NB_N, NB_A)
 
     def timings(self):
         ms = C.c_float(); n = C.c_ulonglong()

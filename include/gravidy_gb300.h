@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define H4_ABI_VERSION 1
+#define H4_ABI_VERSION 2
 
 typedef struct { double x, y, z, w; } h4_double4;
 typedef struct { double x, y, z; } h4_double3;
@@ -97,6 +97,15 @@ int h4_set_force_mode(h4_handle h, int mode);
  * Default 192 for N >= 131072, 320 for N >= 65536, else 768 (measured
  * crossover on GB300). */
 int h4_set_mixed_threshold(h4_handle h, unsigned int nact_threshold);
+
+/* H4_FORCE_FP64 and H4_FORCE_EXACT: h4_advance runs its block steps in one
+ * persistent kernel (one block per SM, grid-wide barriers between the passes
+ * of a step) when N <= max_n, else as one kernel per pass; both give
+ * bit-identical results.  At small N a step is a few microseconds of work and
+ * the per-kernel launch latency dominates.  0 disables the persistent loop.
+ * Default H4_STEP_LOOP_MAX_N_DEFAULT. */
+#define H4_STEP_LOOP_MAX_N_DEFAULT 16384u
+int h4_set_step_loop(h4_handle h, unsigned int max_n);
 
 /* Hermite4GPU::init_acc_jrk (Hermite4GPU.cu:333-375): acc and jerk of all
  * particles from the current predictors (O(N^2)). */
@@ -192,10 +201,16 @@ int h4_forces_for(h4_handle h, const h4_double4 *pr, const h4_double4 *pv,
  * calls above.  Systems are stored back to back: system c owns particles
  * [sum n[0..c), sum n[0..c]) of every concatenated array. */
 typedef struct h4_ensemble_s *h4_ens_handle;
-/* Tuning table: for (N bucket b, active-count bucket a) at index b*NB_A + a:
- * particles per warp item (1, 2 or 4) and j-chunk length.  N buckets:
- * <=512, <=1k, <=2k, <=4k, <=8k, larger; active buckets: 1, 2-3, 4-15,
- * 16-63, 64-255, 256-1023, 1024-4095, >=4096. */
+/* Tuning table: for (N bucket b, active-count bucket a) at index b*NB_A + a,
+ * the shape of the force work of a system's block step.  N buckets: <=512,
+ * <=1k, <=2k, <=4k, <=8k, larger; active buckets: 1, 2-3, 4-15, 16-63,
+ * 64-255, 256-1023, 1024-4095, >=4096.
+ *   ig     FP64 and exact forms: particles per warp item (1, 2 or 4).
+ *          Mixed form: 1 or 2 = warp items (lanes over j; 2 = one packed
+ *          pair), or a power of two in [16, 512] = block-tiled items of ig
+ *          particles (lanes over i, j tiles in shared memory).
+ *   chunk  j per item (rounded up to whole tiles for block items).
+ *   jtile  j per shared-memory tile of a block item, 128 or 256 (NULL: 256). */
 #define H4_ENS_TUNE_NB_N 6
 #define H4_ENS_TUNE_NB_A 8
 const char *h4_ens_last_error(void);
@@ -205,7 +220,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n,
 int h4_ens_destroy(h4_ens_handle e);
 int h4_ens_set_stream(h4_ens_handle e, void *stream);
 int h4_ens_set_tuning(h4_ens_handle e, const unsigned int *ig,
-                      const unsigned int *chunk);
+                      const unsigned int *chunk, const unsigned int *jtile);
 int h4_ens_set_dt_limits(h4_ens_handle e, double dt_min, double dt_max);
 /* init_acc_jrk + init_dt (ETA_S) of every system. */
 int h4_ens_init(h4_ens_handle e);
@@ -225,7 +240,12 @@ int h4_ens_system_stats(h4_ens_handle e, double *itime, double *atime,
  * particles active (positions as stored), using (ig, chunk) everywhere;
  * *ms = device time.  Leaves the integration state unchanged. */
 int h4_ens_tune_force(h4_ens_handle e, unsigned int nact, unsigned int ig,
-                      unsigned int chunk, float *ms);
+                      unsigned int chunk, unsigned int jtile, float *ms);
+/* Block steps and interactions (N_act * N) per tuning bucket, summed over the
+ * systems' steps since creation (index b*NB_A + a as the tuning table): the
+ * mixture of (N, N_act) a tuning should be weighted by.  Either may be NULL. */
+int h4_ens_bucket_stats(h4_ens_handle e, unsigned long long *steps,
+                        unsigned long long *inter);
 int h4_ens_timings(h4_ens_handle e, float *advance_ms,
                    unsigned long long *kernel_launches);
 /* Device time per phase of the persistent ensemble kernel since creation

@@ -139,7 +139,7 @@ def ensemble(mode, sizes, t_end, seed0=300):
         st = E.download()
         en = E.energy()
         stats = E.stats()
-        probe = E.tune_force(2100, 4, 256) if mode == "mixed" else 0.0
+        probe = E.tune_force(2100, 64, 512, 128) if mode == "mixed" else 0.0
     return _h(st["r"], st["v"], st["f"], st["t"], st["dt"], np.asarray(en), stats["steps"]), probe >= 0.0
 
 

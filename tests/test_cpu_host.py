@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
     missing = [s for s in syms if not hasattr(L, s)]
     assert not missing, missing
     assert set(syms) == set(_lib.SIGNATURES), set(syms) ^ set(_lib.SIGNATURES)
-    assert L.h4_abi_version() == 1
+    assert L.h4_abi_version() == 2
 
 
 def test_create_validates_arguments_before_touching_the_device():
