@@ -2,10 +2,12 @@
 
 #include <sys/stat.h>
 
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <ctime>
 #include <iomanip>
+#include <iostream>
 #include <sstream>
 
 #include "Timer.hpp"
@@ -15,7 +17,8 @@ namespace gb300 {
 Logger::Logger(NbodySystem *ns_) : ns(ns_) {
     print_screen = ns->ops.print_screen;
     ofname = ns->output_filename;
-    ofname_info = ofname + ".info";
+    // a run resumed from an info file writes that file again (Logger.cpp:39-50)
+    ofname_info = ns->resume_info ? ns->resume_filename : ofname + ".info";
 }
 
 std::string Logger::get_timestamp() const {
@@ -41,7 +44,26 @@ void Logger::add_info(const std::string &key, const std::string &value) {
          << value << std::endl;
 }
 
+static bool path_exists(const std::string &p) {
+    struct stat b;
+    return stat(p.c_str(), &b) != -1;
+}
+
+// Logger.cpp:136-217: an existing info file is kept as <info>.old, or
+// <info>.old<k> with the first free k, before the new one is written.
 void Logger::write_info() {
+    if (path_exists(ofname_info)) {
+        const char last = ofname_info.empty() ? ' ' : ofname_info.back();
+        std::string newname = ofname_info + ".old";
+        int ext = 0;
+        while (path_exists(newname)) {
+            if (std::isdigit((unsigned char)last)) ext = (last - '0') + 1;
+            newname = ofname_info + ".old" + std::to_string(ext);
+            ext++;
+        }
+        if (std::rename(ofname_info.c_str(), newname.c_str()))
+            std::cerr << "gravidy: Failed to rename info file from " << ofname_info << " to " << newname << std::endl;
+    }
     std::ofstream info(ofname_info.c_str(), std::ios::out);
     info << std::setw(2) << std::left << "#" << std::setw(20) << std::left << "NumberParticles:" << std::setw(20)
          << std::right << ns->n << std::endl;

@@ -15,8 +15,9 @@ NbodySystem::NbodySystem(const OptionsParser &op)
     : gpus(op.gpus), iterations(0), n(0), snapshot_number(op.snapshot_number),
       length_snap(op.length_output_number), force_mode(op.force_mode), host_steps(op.host_steps),
       eta(op.eta), total_mass(0.f), integration_time(op.integration_time), interval_time(op.interval_time),
-      snapshot_time(op.snapshot_time), resume(op.resume), max_mass(0.f), input_filename(op.input_filename),
-      output_filename(op.output_filename), resume_filename(op.resume_filename), h_id(nullptr), h_move(nullptr), h_t(nullptr), h_dt(nullptr),
+      snapshot_time(op.snapshot_time), resume(op.resume), resume_info(op.resume_info), max_mass(0.f),
+      input_filename(op.input_filename), output_filename(op.output_filename), resume_filename(op.resume_filename),
+      snapshot_filename(op.snapshot_filename), h_id(nullptr), h_move(nullptr), h_t(nullptr), h_dt(nullptr),
       h_r(nullptr), h_v(nullptr), h_a2(nullptr), h_a3(nullptr), h_f(nullptr), h_old(nullptr) {
     ops = op.ops;
     // NbodySystem.cpp:50: the product of two floats, kept as a float.
@@ -32,9 +33,11 @@ bool NbodySystem::read_input_file() {
     total_mass = 0;
     max_mass = 0.0f;
     bool got_time = false;
-    std::ifstream file(input_filename.c_str());
+    // a resumed run reads the snapshot the info file names (NbodySystem.cpp:86-95)
+    const std::string &path = resume_info ? snapshot_filename : input_filename;
+    std::ifstream file(path.c_str());
     if (!file.is_open()) {
-        std::cerr << "gravidy: cannot open " << input_filename << std::endl;
+        std::cerr << "gravidy: cannot open " << path << std::endl;
         return false;
     }
     std::string line;
@@ -63,7 +66,7 @@ bool NbodySystem::read_input_file() {
             std::vector<std::string> tok((std::istream_iterator<std::string>(iss)),
                                          std::istream_iterator<std::string>());
             if (tok.size() != 8) {
-                std::cerr << "gravidy: wrong line format in " << input_filename
+                std::cerr << "gravidy: wrong line format in " << path
                           << ": only eight numbers per line are allowed" << std::endl;
                 break;
             }

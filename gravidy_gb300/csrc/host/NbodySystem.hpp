@@ -42,12 +42,14 @@ class NbodySystem {
     double e2;
     double snapshot_time;
     bool resume;
+    bool resume_info;               // resumed from a reference .info file: read snapshot_filename
     Energy en;
     float max_mass;
 
     std::string input_filename;
     std::string output_filename;
     std::string resume_filename;
+    std::string snapshot_filename;
 
     // Host mirrors (NbodySystem.hpp:112-128).
     unsigned int *h_id;

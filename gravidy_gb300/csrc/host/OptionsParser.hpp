@@ -2,7 +2,10 @@
 // OptionsParser.hpp:50-79, flags and defaults of OptionsParser.cpp:41-81 and
 // :329-421), parsed without boost.  Added flags: --mode fp64|exact|mixed
 // selects the force arithmetic, --host-steps drives the block steps one by
-// one from the host instead of the device-resident loop.
+// one from the host instead of the device-resident loop.  -r takes either
+// this program's exact checkpoint (<out>.chk) or, as the reference does, an
+// <out>.info file (OptionsParser.cpp:122-323): the run restarts from the
+// snapshot that file names.
 #ifndef GRAVIDY_GB300_HOST_OPTIONSPARSER_HPP
 #define GRAVIDY_GB300_HOST_OPTIONSPARSER_HPP
 
@@ -29,6 +32,7 @@ class OptionsParser {
     unsigned int snapshot_number;
     unsigned int length_output_number;
     bool resume;
+    bool resume_info;   // resume from the reference's <out>.info and its 4-digit snapshot
     options ops;
     int force_mode;
     bool host_steps;
@@ -38,6 +42,7 @@ class OptionsParser {
     std::string usage() const;
 
   private:
+    bool read_info(bool have_time, bool have_softening, bool have_eta, bool have_screen);
     int argc_;
     char **argv_;
 };

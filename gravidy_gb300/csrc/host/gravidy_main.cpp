@@ -14,7 +14,8 @@ int main(int argc, char *argv[]) {
     if (!op.check_options()) return 1;
     NbodySystem ns(op);
     CheckpointScalars chk{};
-    if (op.resume) {
+    const bool exact_resume = op.resume && !op.resume_info;
+    if (exact_resume) {
         // exact continuation: state and loop counters from the checkpoint
         if (!read_checkpoint(op.resume_filename, ns, chk)) return 1;
     } else {
@@ -24,7 +25,7 @@ int main(int argc, char *argv[]) {
     }
     Logger logger(&ns);
     try {
-        if (op.resume) {
+        if (exact_resume) {
             Hermite4GPU h4(&ns, &logger, chk);
             h4.integration();
         } else {

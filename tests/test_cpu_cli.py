@@ -47,3 +47,30 @@ def test_no_device_is_a_clean_error(tmp_path):
     r = _run("-i", inp, "-t", "0.125", "-o", str(tmp_path / "run"))
     assert r.returncode not in (0, -11, 139)   # an error status, not success and not SIGSEGV
     assert "CUDA" in r.stdout + r.stderr
+
+
+def _info(path, **over):
+    keys = {"NumberParticles": "33", "Softening": "0.05", "EtaTimestep": "0.01", "IntegrationTime": "0.0625",
+            "PrintScreen": "0", "InputFilename": str(path / "in.txt"), "OutputFilename": str(path / "run.out"),
+            "SnapshotNumber": "7"}
+    keys.update(over)
+    with open(path / "run.out.info", "w") as fh:
+        for k, v in keys.items():
+            fh.write(f"# {k + ':':<20}{v:>20}\n")
+    return str(path / "run.out.info")
+
+
+def test_resume_from_info_file_arguments(tmp_path):
+    """-r <out>.info follows the reference's resume rules
+    (OptionsParser.cpp:122-323) before any device work: -t is required and
+    must exceed the info file's IntegrationTime, every key must be known, and
+    the snapshot it names (4-digit counter) must exist."""
+    info = _info(tmp_path)
+    r = _run("-r", info)
+    assert r.returncode != 0 and "'time'" in r.stderr
+    r = _run("-r", info, "-t", "0.0625")
+    assert r.returncode != 0 and "greater than the one" in r.stderr
+    r = _run("-r", info, "-t", "0.125")
+    assert r.returncode != 0 and "run.out.snapshot_0007" in r.stderr
+    r = _run("-r", _info(tmp_path, Colour="blue"), "-t", "0.125")
+    assert r.returncode != 0 and "Invalid option -- Colour" in r.stderr

@@ -72,3 +72,36 @@ def test_cli_lagrange_radii_file(tmp_path):
         if line.startswith("t0_lagr"):
             want = [float.fromhex(t) for t in line.split()[1:7]]
     assert [float(x) for x in rows[0][2:8]] == pytest.approx(want, rel=1e-5, abs=1e-6)
+
+
+def test_cli_resume_from_info_file(tmp_path):
+    """-r <out>.info (the reference's resume, OptionsParser.cpp:122-323):
+    the run restarts at the info file's time from the snapshot it names and
+    logs to <input>.out.log; in the exact mode that log equals, bit for bit in
+    its deterministic columns, a fresh run whose input is that snapshot file
+    (its "# Time:" header sets the start time).  The old info file is kept as
+    <info>.old."""
+    build_library()
+    build_cli()
+    name = "salpeter_n100"
+    c = cases()[name]
+    inp = tmp_path / "in.txt"
+    inp.write_text(open(os.path.join(case_dir(name), "input.txt")).read())
+    common = ["-s", repr(c["softening"]), "-e", repr(c["eta"]), "-z", repr(2.0 ** -11), "--mode", "exact"]
+    r = subprocess.run([CLI, "-i", str(inp), "-t", repr(2.0 ** -4), "-o", str(tmp_path / "run"), *common],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    info = {l.split(":")[0].strip("# "): l.split(":", 1)[1].strip() for l in open(tmp_path / "run.out.info")}
+    snap = tmp_path / f"run.out.snapshot_{int(info['SnapshotNumber']):04d}"
+    assert snap.exists()
+    r = subprocess.run([CLI, "-r", str(tmp_path / "run.out.info"), "-t", repr(2.0 ** -3), *common],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert (tmp_path / "run.out.info.old").exists()
+    resumed = [l.split()[1:7] for l in open(str(inp) + ".out.log") if not l.startswith("#")]
+    r = subprocess.run([CLI, "-i", str(snap), "-t", repr(2.0 ** -3), "-o", str(tmp_path / "fresh"), *common],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    fresh = [l.split()[1:7] for l in open(tmp_path / "fresh.out.log") if not l.startswith("#")]
+    assert len(resumed) > 1 and resumed == fresh
+    assert float(resumed[0][0]) == pytest.approx(2.0 ** -4)
