@@ -982,18 +982,19 @@ void ens_free(h4_ensemble_s *E) {
 // Default tuning table (used until a tuned table is loaded).  FP64: up to 4
 // particles per warp item; j-chunks short for small active sets (more
 // items), the whole system for large ones.  Mixed: warp items of a packed
-// pair below 64 active particles, block-tiled items above (wider ones for
-// larger active sets), 2048 j per item, tiles of 256.
+// pair below 1024 active particles, block-tiled items of 512 particles above,
+// 1024 j per block item (many items per step: in an ensemble few systems
+// take a large step in the same iteration), tiles of 256.
 void default_tuning(int mode, unsigned *ig, unsigned *chunk, unsigned *jt) {
     static const unsigned ch[NB_A] = {128, 128, 256, 512, 1024, 2048, 4096, 8192};
-    static const unsigned mixed_ig[NB_A] = {1, 2, 2, 2, 64, 256, 512, 512};
+    static const unsigned mixed_ig[NB_A] = {1, 2, 2, 2, 2, 2, 512, 512};
     for (int b = 0; b < NB_N; b++) {
         for (int a = 0; a < NB_A; a++) {
             const int t = b * NB_A + a;
             jt[t] = JT_MAX;
             if (mode == H4_FORCE_MIXED) {
                 ig[t] = mixed_ig[a];
-                chunk[t] = mixed_ig[a] > 2 ? 2048 : ch[a];
+                chunk[t] = mixed_ig[a] > 2 ? 1024 : ch[a];
             } else {
                 ig[t] = 4;
                 chunk[t] = ch[a];

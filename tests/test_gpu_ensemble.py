@@ -141,7 +141,7 @@ def test_ensemble_mixed_forces_vs_oracle():
         ea = rel_err_vec(got[:, :3], want[:, :3])
         ej = rel_err_vec(got[:, 3:], want[:, 3:])
         assert np.median(ea) < 1e-6 and ea.max() < 1e-4, (c, np.median(ea), ea.max())
-        assert np.median(ej) < 1e-6 and ej.max() < 1e-3, (c, np.median(ej), ej.max())
+        assert np.median(ej) < 1e-6 and ej.max() < 1e-4, (c, np.median(ej), ej.max())
 
 
 def test_ensemble_mixed_forces_large_system_vs_oracle():
@@ -163,7 +163,7 @@ def test_ensemble_mixed_forces_large_system_vs_oracle():
         print(f"N={len(m)}: acc median {np.median(ea):.2e} max {ea.max():.2e}; "
               f"jerk median {np.median(ej):.2e} max {ej.max():.2e}")
         assert np.median(ea) < 1e-6 and ea.max() < 1e-4, (c, np.median(ea), ea.max())
-        assert np.median(ej) < 1e-6 and ej.max() < 1e-3, (c, np.median(ej), ej.max())
+        assert np.median(ej) < 1e-6 and ej.max() < 1e-4, (c, np.median(ej), ej.max())
 
 
 def test_ensemble_phase_timers():
