@@ -33,7 +33,6 @@ SIGNATURES = {
     "h4_set_dt_limits": (_i, [_vp, _d, _d]),
     "h4_set_force_mode": (_i, [_vp, _i]),
     "h4_set_mixed_threshold": (_i, [_vp, _u]),
-    "h4_set_step_loop": (_i, [_vp, _u]),
     "h4_init_acc_jrk": (_i, [_vp]),
     "h4_init_dt": (_i, [_vp, _pd, _f, _d]),
     "h4_find_particles_to_move": (_i, [_vp, _d, _pu]),

@@ -32,7 +32,7 @@ CLI = os.path.join(BUILD, "gravidy-gb300")
 BOUNDS_LIB = os.path.join(BUILD, "bounds", "libgravidy_gb300.so")
 
 CUDA_SOURCES = ["h4_capi.cu", "h4_step_kernels.cu", "h4_force_fp64.cu", "h4_energy.cu", "h4_probe.cu",
-                "h4_noalloc.cu", "h4_force_mixed.cu", "h4_ensemble.cu", "h4_diagnostics.cu", "h4_step_loop.cu"]
+                "h4_noalloc.cu", "h4_force_mixed.cu", "h4_ensemble.cu", "h4_diagnostics.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 # Extra nvcc flags (e.g. -D build knobs of the kernels), space separated.

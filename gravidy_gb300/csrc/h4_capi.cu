@@ -81,9 +81,6 @@ struct h4_system_s {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_mode = -1;
-    bool graph_loop = false;        // the graph's body is the persistent step loop
-    unsigned loop_max_n = 0;        // h4_advance runs the persistent step loop for N <= this
-    int loop_grid = 0;              // blocks of the persistent step loop (0: not available)
     unsigned mixed_threshold = 0;   // set at creation from N
     PhaseTimer phase[PH_COUNT];
     cudaStream_t graph_stream = nullptr;
@@ -199,17 +196,8 @@ void enqueue_step(h4_system_s *h, cudaStream_t s, const cudaGraphConditionalHand
 // Kernels in one captured block step (force kernels counted per mode).
 int step_kernel_count(const h4_system_s *h) { return 4 + (h->mode == H4_FORCE_MIXED ? 2 : 1); }
 
-// Block steps one persistent step-loop launch runs before the graph's
-// while-loop node relaunches it.
-constexpr int LOOP_ITERS = 64;
-
-bool use_step_loop(const h4_system_s *h) {
-    return step_loop_supported(h->mode) && h->loop_grid > 0 && (unsigned)h->d.n <= h->loop_max_n;
-}
-
 int build_graph(h4_system_s *h) {
-    const bool loop = use_step_loop(h);
-    if (h->graph_exec && h->graph_mode == h->mode && h->graph_loop == loop) return H4_OK;
+    if (h->graph_exec && h->graph_mode == h->mode) return H4_OK;
     if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
     if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
     if (!h->graph_stream) H4_TRY(cudaStreamCreateWithFlags(&h->graph_stream, cudaStreamNonBlocking), "graph stream");
@@ -228,20 +216,13 @@ int build_graph(h4_system_s *h) {
                                          cudaStreamCaptureModeThreadLocal),
            "begin capture");
     unsigned long long saved = h->launches;
-    cudaError_t le = cudaSuccess;
-    if (loop)
-        le = launch_step_loop(h->d, h->mode, h->loop_grid, LOOP_ITERS, (unsigned)grid_warps(h), cond,
-                              h->graph_stream);
-    else
-        enqueue_step(h, h->graph_stream, &cond);
+    enqueue_step(h, h->graph_stream, &cond);
     h->launches = saved;
     cudaGraph_t captured = nullptr;
     cudaError_t e = cudaStreamEndCapture(h->graph_stream, &captured);
-    if (le != cudaSuccess) return cuda_fail(le, "capture step loop");
     if (e != cudaSuccess) return cuda_fail(e, "end capture");
     H4_TRY(cudaGraphInstantiate(&h->graph_exec, h->graph, 0), "cudaGraphInstantiate");
     h->graph_mode = h->mode;
-    h->graph_loop = loop;
     return H4_OK;
 }
 
@@ -299,7 +280,6 @@ int h4_create(h4_handle *out, unsigned int n, double e2, float eta, const h4_dou
     h->mode = mode;
     d.mixed = mode == H4_FORCE_MIXED ? 1 : 0;
     h->mixed_threshold = default_mixed_threshold(n);
-    h->loop_max_n = H4_STEP_LOOP_MAX_N_DEFAULT;
     const size_t N = n, NP = (size_t)d.n_pad;
     d.part_cap = 6 * (N + 262144);
     const int nflag = (int)((N + FLAG_CHUNK - 1) / FLAG_CHUNK);
@@ -326,7 +306,6 @@ int h4_create(h4_handle *out, unsigned int n, double e2, float eta, const h4_dou
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev2);
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev3);
-    if (e == cudaSuccess) e = step_loop_max_grid(H4_FORCE_FP64, h->num_sms, &h->loop_grid);
     if (e != cudaSuccess) { free_device(h); delete h; return cuda_fail(e, "h4_create: setup"); }
     h->stream = h->own_stream;
     cudaStream_t s = h->stream;
@@ -406,12 +385,6 @@ int h4_set_mixed_threshold(h4_handle h, unsigned int nact_threshold) {
     if (nact_threshold < 1) return fail(H4_ERR_ARG, "threshold must be >= 1");
     h->mixed_threshold = nact_threshold;
     if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; h->graph_mode = -1; }
-    return H4_OK;
-}
-
-int h4_set_step_loop(h4_handle h, unsigned int max_n) {
-    if (!h) return fail(H4_ERR_ARG, "null handle");
-    h->loop_max_n = max_n;
     return H4_OK;
 }
 
@@ -581,8 +554,6 @@ int h4_advance(h4_handle h, double t_stop, double t_log, double *atime, double *
     c.t_log = t_log;
     c.steps = c.psteps = c.inter = 0;
     c.running = 1;
-    c.bar_count = 0;
-    c.loop_launches = 0;
     {
         const double t0 = atime ? *atime : bits_to_double_host(c.atime_bits);
         double span = (t_stop < t_log ? t_stop : t_log) - t0;
@@ -600,8 +571,7 @@ int h4_advance(h4_handle h, double t_stop, double t_log, double *atime, double *
     h->phase[PH_ADVANCE].total_ms += h->last_advance_ms;
     h->phase[PH_ADVANCE].count += 1;
     const H4Ctrl &o = *h->h_ctrl;
-    h->launches += h->graph_loop ? o.loop_launches
-                                 : (unsigned long long)o.steps * (unsigned long long)step_kernel_count(h);
+    h->launches += (unsigned long long)o.steps * (unsigned long long)step_kernel_count(h);
     if (atime) *atime = bits_to_double_host(o.atime_bits);
     if (itime) *itime = o.itime;
     if (stats) {

@@ -1003,6 +1003,19 @@ void default_tuning(int mode, unsigned *ig, unsigned *chunk, unsigned *jt) {
     }
 }
 
+// Partial-force area of a system of n particles (doubles): room for
+// `splits` j-chunks of every particle, so that a step with all particles
+// active still splits into enough items to fill the GPU (a block step of one
+// large system often runs with few other systems stepping), and for 4096
+// partials beyond that for the many-chunk splits of small active sets.
+// splits = 16, fewer for ensembles of more than 2^22 particles (about 0.8 GB
+// of partials at 2^22; at least one chunk per particle).
+size_t part_splits_for(size_t total) {
+    const size_t s = ((size_t)1 << 26) / (total ? total : 1);
+    return s < 1 ? 1 : (s > 16 ? 16 : s);
+}
+size_t part_cap_for(unsigned n, size_t splits) { return 6 * (splits * (size_t)n + 4096); }
+
 // Checks a tuning table for the ensemble's force mode (see h4_ens_set_tuning).
 bool tuning_valid(int mode, const unsigned *ig, const unsigned *chunk, const unsigned *jt) {
     for (int t = 0; t < NB_N * NB_A; t++) {
@@ -1068,8 +1081,9 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
         if (n[c] < 1 || n[c] > (1u << 24)) return efail(H4_ERR_ARG, "h4_ens_create: system size out of range");
         if (!(e2[c] >= 0.0) || !(eta[c] > 0.f)) return efail(H4_ERR_ARG, "h4_ens_create: bad e2 or eta");
         total += n[c];
-        part_total += 6 * ((size_t)n[c] + 4096);
     }
+    const size_t splits = part_splits_for(total);
+    for (unsigned c = 0; c < nsys; c++) part_total += part_cap_for(n[c], splits);
     if (total > (1u << 28)) return efail(H4_ERR_ARG, "h4_ens_create: too many particles");
     for (size_t i = 0; i < total; i++)
         if (!std::isfinite(r[i].x) || !std::isfinite(r[i].y) || !std::isfinite(r[i].z) || !std::isfinite(r[i].w) ||
@@ -1103,7 +1117,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
         S.dt_max = 0.125;
         S.t_end = 0.0;
         S.part_off = poff;
-        S.part_cap = 6 * ((size_t)n[c] + 4096);
+        S.part_cap = part_cap_for(n[c], splits);
         E->host_sys[c] = S;
         off += n[c];
         poff += S.part_cap;

@@ -1,7 +1,7 @@
-// FP64 force sum of the active particles as a device routine: shared by the
-// force kernel (h4_force_fp64.cu) and the persistent step loop
-// (h4_step_loop.cu), which must produce the same work items, and hence the
-// same summation order, from the same active set.
+// FP64 force sum of the active particles as device routines (the work-item
+// loop of k_force_fp64 and the exact per-particle sum of k_force_exact); any
+// launch shape yields the same items, and hence the same summation order,
+// from the same active set.
 #pragma once
 #include "h4_internal.cuh"
 #include "h4_pair.cuh"
@@ -18,6 +18,11 @@ namespace fp64 {
 constexpr int WARPS = 4;        // warps per block of the force kernel
 constexpr int IG = H4_FP64_IG;  // active particles per work item (build knob: 2, 4 or 8)
 constexpr int ITEMS_PER_WARP = 12;
+// Smaller items for small steps (build knob; 0 = always IG particles, >= 64 j).
+#ifndef H4_FP64_SMALL_SPLIT
+#define H4_FP64_SMALL_SPLIT 1
+#endif
+constexpr bool kFp64SmallSplit = H4_FP64_SMALL_SPLIT != 0;
 
 // Warp `warp` (lane `lane`) of `nwarps` takes work items from the queue in
 // the control block until it is empty.  The j-split is fixed by nact, n and
@@ -28,9 +33,18 @@ constexpr int ITEMS_PER_WARP = 12;
 __device__ __forceinline__ void force_items(const H4Dev &d, unsigned split_warps, int lane, bool first) {
     const unsigned nact = d.ctrl->nact;
     if (nact == 0) return;
-    const unsigned n_groups = (nact + IG - 1) / IG;
+    // Small steps (too few items of IG particles and >= 64 j to give every
+    // warp one): fewer particles per item, then chunks down to 32 j, so that
+    // each warp's FP64 chain is short -- at 1/64 of the FP32 rate the step is
+    // then bound by the longest chain, not by the total work.
+    unsigned ig = IG, min_chunk = 64;
+    if (kFp64SmallSplit) {
+        while (ig > 1 && ((nact + ig - 1) / ig) * (unsigned)((d.n + 63) / 64) < split_warps) ig >>= 1;
+        if (ig == 1 && nact * (unsigned)((d.n + 63) / 64) < split_warps) min_chunk = 32;
+    }
+    const unsigned n_groups = (nact + ig - 1) / ig;
     unsigned split = (split_warps * ITEMS_PER_WARP + n_groups - 1) / n_groups;
-    unsigned max_split = (unsigned)((d.n + 63) / 64);
+    unsigned max_split = (unsigned)((d.n + min_chunk - 1) / min_chunk);
     if (split > max_split) split = max_split;
     const unsigned cap_split = (unsigned)(d.part_cap / (6ull * nact));
     if (split > cap_split) split = cap_split;
@@ -52,8 +66,8 @@ __device__ __forceinline__ void force_items(const H4Dev &d, unsigned split_warps
         const unsigned g = item - s * n_groups;
         const int j_begin = (int)s * chunk;
         const int j_end = min(d.n, j_begin + chunk);
-        const unsigned k0 = g * IG;
-        const unsigned cnt = min((unsigned)IG, nact - k0);
+        const unsigned k0 = g * ig;
+        const unsigned cnt = min(ig, nact - k0);
         double *part_s = d.part + (size_t)s * 6 * nact;
         if (kBoundsCheck && !pair::warp_item_ok(d, nact, k0, cnt, j_begin, j_end, s, lane, BS_FP64_J)) continue;
         if (cnt == (unsigned)IG) {

@@ -38,8 +38,6 @@ struct H4Ctrl {
     unsigned long long nact_hist[32]; // block steps by floor(log2(nact)), since creation
     int running;                   // 1 while the device loop continues
     unsigned int bounds_site;      // first failing check of the bounds-checked build (0 = none)
-    unsigned int bar_count, bar_gen;   // grid barrier of the persistent step loop
-    unsigned long long loop_launches;  // persistent step-loop launches of the current h4_advance
 };
 
 enum : unsigned int {
@@ -178,15 +176,6 @@ void launch_force_exact(const H4Dev &d, cudaStream_t s);   // writes d.part with
 int launch_force_mixed(const H4Dev &d, int num_sms, unsigned threshold, long long known_nact, cudaStream_t s);
 
 int force_fp64_grid_warps(int num_sms);
-
-// ---- persistent step loop (h4_step_loop.cu) -----------------------------------
-// One cooperative kernel runs up to max_iters whole block steps of h4_advance
-// (FP64 and exact forms); split_warps = force_fp64_grid_warps(num_sms), so the
-// force items match k_force_fp64's.  Sets `cond` when it stops.
-int step_loop_supported(int mode);
-cudaError_t launch_step_loop(const H4Dev &d, int mode, int grid, int max_iters, unsigned split_warps,
-                             cudaGraphConditionalHandle cond, cudaStream_t s);
-cudaError_t step_loop_max_grid(int mode, int num_sms, int *grid);
 
 // ---- energy (h4_energy.cu) --------------------------------------------------
 void launch_energy(const H4Dev &d, cudaStream_t s);

@@ -1,7 +1,6 @@
-// Per-particle pieces of the block step shared by the kernels of one step
-// (h4_step_kernels.cu) and the persistent step loop (h4_step_loop.cu): the
-// predictor, the fused reduction + corrector, and the j data of the mixed
-// form.  Grid-wide loops use the launch's gridDim/blockDim.
+// Per-particle pieces of the block step (h4_step_kernels.cu): the predictor,
+// the fused reduction + corrector, and the j data of the mixed form.
+// Grid-wide loops use the launch's gridDim/blockDim.
 #pragma once
 #include "h4_exact.cuh"
 #include "h4_internal.cuh"

@@ -280,11 +280,6 @@ class Hermite4GPU:
     def set_mixed_threshold(self, nact_threshold: int):
         _lib.check(self.L.h4_set_mixed_threshold(self.h, int(nact_threshold)))
 
-    def set_step_loop(self, max_n: int):
-        """h4_advance runs its block steps in one persistent kernel when
-        N <= max_n (FP64 and exact forms; 0 = one kernel per pass)."""
-        _lib.check(self.L.h4_set_step_loop(self.h, max_n))
-
     def set_force_mode(self, mode: str):
         _lib.check(self.L.h4_set_force_mode(self.h, _lib.MODES[mode]))
         self.mode = mode

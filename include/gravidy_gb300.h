@@ -98,15 +98,6 @@ int h4_set_force_mode(h4_handle h, int mode);
  * crossover on GB300). */
 int h4_set_mixed_threshold(h4_handle h, unsigned int nact_threshold);
 
-/* H4_FORCE_FP64 and H4_FORCE_EXACT: h4_advance runs its block steps in one
- * persistent kernel (one block per SM, grid-wide barriers between the passes
- * of a step) when N <= max_n, else as one kernel per pass; both give
- * bit-identical results.  At small N a step is a few microseconds of work and
- * the per-kernel launch latency dominates.  0 disables the persistent loop.
- * Default H4_STEP_LOOP_MAX_N_DEFAULT. */
-#define H4_STEP_LOOP_MAX_N_DEFAULT 16384u
-int h4_set_step_loop(h4_handle h, unsigned int max_n);
-
 /* Hermite4GPU::init_acc_jrk (Hermite4GPU.cu:333-375): acc and jerk of all
  * particles from the current predictors (O(N^2)). */
 int h4_init_acc_jrk(h4_handle h);

@@ -118,17 +118,32 @@ def test_header_constants_match_the_binding():
 
 
 def test_committed_tuning_table_is_well_formed():
-    """gravidy_gb300/tuning/ensemble_gb300.json: one (ig, chunk) table per
-    force form, NB_N x NB_A entries, ig in {1, 2, 4}, chunks multiples of 32."""
+    """gravidy_gb300/tuning/ensemble_gb300.json: one table per force form
+    covering every (N, N_act) bucket (NB_N x NB_A entries).  FP64: ig in
+    {1, 2, 4}, chunks multiples of 32.  Mixed: ig 1 or 2 (warp items) or a
+    power of two in [16, 512] (block-tiled items), j tiles of 128 or 256 and
+    block-item chunks a whole number of tiles; the mixture weights the tuner
+    recorded have the same shape."""
     import json
     from gravidy_gb300 import ensemble
     t = json.load(open(ensemble.TUNING_FILE))
+    shape = (ensemble.NB_N, ensemble.NB_A)
     for mode in ("fp64", "mixed"):
-        ig = np.array(t["modes"][mode]["ig"])
-        ch = np.array(t["modes"][mode]["chunk"])
-        assert ig.shape == ch.shape == (ensemble.NB_N, ensemble.NB_A)
-        assert set(np.unique(ig)) <= {1, 2, 4}
+        T = t["modes"][mode]
+        ig = np.array(T["ig"])
+        ch = np.array(T["chunk"])
+        jt = np.array(T.get("jtile", np.full(shape, 256)))
+        assert ig.shape == ch.shape == jt.shape == shape
         assert np.all(ch >= 32) and np.all(ch % 32 == 0)
+        if mode == "fp64":
+            assert set(np.unique(ig)) <= {1, 2, 4}
+        else:
+            assert "jtile" in T
+            assert set(np.unique(ig)) <= {1, 2, 16, 32, 64, 128, 256, 512}
+            assert set(np.unique(jt)) <= {128, 256}
+            block = ig >= 16
+            assert np.all(ch[block] % jt[block] == 0)
+            assert np.array(T["c4_interactions"]).shape == shape
 
 
 def test_c4_sizes_are_seeded_and_in_range():

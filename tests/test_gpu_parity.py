@@ -194,34 +194,6 @@ def test_advance_graph_equals_host_driven_steps():
             assert np.array_equal(sa[k], sb[k]), k
 
 
-@pytest.mark.parametrize("mode,n,t_end", [("fp64", 3000, 0.0625), ("fp64", 17, 0.125), ("exact", 300, 0.03125)])
-def test_step_loop_equals_one_kernel_per_pass(mode, n, t_end):
-    """h4_advance in one persistent kernel (grid-wide barriers between the
-    passes of a step) and with one kernel per pass: the same block steps,
-    counters and, bit for bit, the same state; the log stops (t_log) land on
-    the same steps."""
-    ns = plummer_system(n, seed=21, imf="salpeter")
-    with Hermite4GPU(ns, mode=mode) as a, Hermite4GPU(ns, mode=mode) as b:
-        a.set_step_loop(1 << 20)
-        b.set_step_loop(0)
-        for g in (a, b):
-            g.init_acc_jrk()
-        ta, tb = a.init_dt(), b.init_dt()
-        assert ta == tb
-        ia = ib = 0.0
-        for k in range(1, 5):   # four log intervals
-            t_log = t_end * k / 4
-            ia, ta, *ra = a.advance(t_end, t_log, ta)
-            ib, tb, *rb = b.advance(t_end, t_log, tb)
-            assert (ia, ta, ra) == (ib, tb, rb), k
-        assert ia >= t_end
-        sa, sb = a.download(), b.download()
-        for key in ("r", "v", "f", "old", "a2", "a3", "t", "dt"):
-            assert np.array_equal(sa[key], sb[key]), key
-        assert np.array_equal(a.nact_histogram(), b.nact_histogram())
-        assert a.get_energy_gpu() == b.get_energy_gpu()
-
-
 @pytest.mark.gpu
 def test_phase_timers_count_host_driven_calls():
     """Per-phase device timers (the reference's Gtime phases, common.hpp:287-310)."""
