@@ -68,6 +68,16 @@ constexpr unsigned MAX_SYSTEMS = 4096;
 constexpr int JT_MAX = 256;
 constexpr unsigned BTI_MIN = 16, BTI_MAX = 2 * THREADS;
 constexpr unsigned WAIT_LIMIT = 1u << 26;  // mbarrier polls before a tile wait gives up
+// Stages in flight: NS block-item tiles per block; per warp, WARP_STAGES
+// stages of WARP_STAGE_J j for the warp items.  The two share one shared-memory
+// area (a block runs its block items, then its warp items).
+constexpr unsigned NS = 3;          // block-item tile stages
+constexpr int WARP_STAGES = 3;      // warp-item stages (per warp)
+constexpr int WARP_STAGE_J = 64;    // j per warp-item stage (two per lane)
+constexpr size_t BLOCK_TILE_BYTES = (size_t)NS * 5 * JT_MAX * sizeof(float4);
+constexpr size_t WARP_RING_BYTES = (size_t)WARP_STAGES * 3 * WARP_STAGE_J * sizeof(float4);
+constexpr size_t TILE_AREA_BYTES =
+    BLOCK_TILE_BYTES > WARPS * WARP_RING_BYTES ? BLOCK_TILE_BYTES : WARPS * WARP_RING_BYTES;
 
 struct System {
     int off, n;                  // particle offset and count
@@ -415,74 +425,41 @@ __device__ __forceinline__ int find_seg(const unsigned *pre, int m, unsigned x) 
     return lo;
 }
 
-// ---- P1: one warp item of some system's force sum ---------------------------
-template <int MODE>
-__device__ void force_item(const Dev &d, const System &S, unsigned local, int lane) {
-    const unsigned s = local / S.n_groups;
-    const unsigned g = local - s * S.n_groups;
-    const int off = S.off;
-    const int jb = (int)(s * S.chunk);
-    const int je = min(S.n, jb + (int)S.chunk);
-    const unsigned nact = S.nact;
-    double *part_s = d.part + S.part_off + (size_t)s * 6 * nact;
-    const unsigned *move = d.move + off;
-    if (MODE == H4_FORCE_EXACT) {
-        const unsigned k = g * 32 + lane;
-        const unsigned cnt = min(32u, nact - g * 32);
-        if (kBoundsCheck && !__all_sync(0xffffffffu, item_ok(d, S, s, g * 32, cnt, 0, S.n, (unsigned)lane))) return;
-        if (k < nact) {
-            double f[6];
-            pair::exact_sum(d.pr + off, d.pv + off, S.n, move[k], S.e2, f);
-#pragma unroll
-            for (int c = 0; c < 6; c++) part_s[(size_t)c * nact + k] = f[c];
-        }
-        return;
-    }
-    const unsigned k0 = g * S.ig;
-    const unsigned cnt = min(S.ig, nact - k0);
-    if (kBoundsCheck && !__all_sync(0xffffffffu, item_ok(d, S, s, k0, cnt, jb, je, (unsigned)lane))) return;
-    if (MODE == H4_FORCE_FP64) {
-        const dbl4 *pr = d.pr + off, *pv = d.pv + off;
-        if (cnt == 4) {
-            pair::fp64_warp_item<4>(pr, pv, move, nact, k0, jb, je, S.e2, part_s, lane);
-        } else {
-            unsigned k = k0;
-            if (cnt >= 2) { pair::fp64_warp_item<2>(pr, pv, move, nact, k, jb, je, S.e2, part_s, lane); k += 2; }
-            if (cnt & 1) pair::fp64_warp_item<1>(pr, pv, move, nact, k, jb, je, S.e2, part_s, lane);
-        }
-    } else {
-        const float4 *a = d.jf0 + off, *b = d.jf1 + off, *c = d.jf2 + off;
-        const float e2 = (float)S.e2;
-        if (S.e2 > 0.0) {   // a packed pair, or one particle
-            if (cnt == 2)
-                pair::mixed_warp_item_x2(a, b, c, move, nact, k0, jb, je, e2, part_s, lane);
-            else
-                pair::mixed_warp_item<1, false>(a, b, c, move, nact, k0, jb, je, e2, part_s, lane);
-        } else {
-            unsigned k = k0;
-            while (k < k0 + cnt) {
-                pair::mixed_warp_item<1, true>(a, b, c, move, nact, k, jb, je, e2, part_s, lane);
-                k++;
-            }
-        }
-    }
-}
-
 // ---- P1 (mixed form): one block-tiled item --------------------------------------
 // S.ig active particles (P = S.ig / 2 packed pairs, one per thread of each of
 // the Q = S.q j-lanes) against one j-chunk of the system's padded j data; the
 // chunk streams through shared memory in tiles of JT j, each tile brought in
 // by five 1-D bulk copies (TMA, one per plane of the duplicated j data) that
-// complete on an mbarrier, double buffered across the block's items.  j past
-// the system's end are zero-mass padding (exact zero terms); needs e2 > 0
-// (the self term is then an exact zero).  Sums as k_force_mixed_tiled_x2:
-// FP32 over runs of at most 64 j per thread, Kahan across runs, stored as
-// doubles, j-lane q of chunk s as partial s * Q + q.  gt counts the tiles
-// this block has consumed (buffer gt & 1, parity (gt >> 1) & 1).  Returns
-// false when a tile wait timed out (the error bit is then set).
+// complete on the stage's `full` mbarrier.  NS stages rotate across the
+// block's items; a warp done with a tile arrives on the stage's `empty`
+// mbarrier, and thread 0 refills a stage once all warps have released it, so
+// the warps of a block may drift apart by up to NS - 1 tiles instead of
+// meeting at a barrier after every tile.  j past the system's end are
+// zero-mass padding (exact zero terms); needs e2 > 0 (the self term is then
+// an exact zero).  Sums as k_force_mixed_tiled_x2: FP32 over runs of at most
+// 64 j per thread, Kahan across runs, stored as doubles, j-lane q of chunk s
+// as partial s * Q + q.  gt counts the tiles this block has consumed (stage
+// gt % NS, phase parity (gt / NS) & 1).  Returns false when a wait timed out
+// (the error bit is then set); the block meets at one barrier per item.
+
+// Thread 0: tile t of the item (global tile g of this block) into stage
+// g % NS, once every warp has released that stage's previous tile.
+template <int JT>
+__device__ __forceinline__ bool issue_tile(float4 (*sj)[5][JT_MAX], uint64_t *full, uint64_t *empty, unsigned g,
+                                           const float4 *src, size_t jtp, int t) {
+    const unsigned b = g % NS;
+    if (g >= NS && !tma::wait_bounded(&empty[b], ((g / NS) - 1u) & 1u, WAIT_LIMIT)) return false;
+    tma::fence_proxy_async();
+    tma::mbar_arrive_expect_tx(&full[b], 5 * JT * (unsigned)sizeof(float4));
+#pragma unroll
+    for (int pl = 0; pl < 5; pl++)
+        tma::load_1d(&sj[b][pl][0], src + pl * jtp + (size_t)t * JT, JT * (unsigned)sizeof(float4), &full[b]);
+    return true;
+}
+
 template <int JT>
 __device__ bool block_item(const Dev &d, const System &S, unsigned local, float4 (*sj)[5][JT_MAX], uint64_t *full,
-                           unsigned &gt) {
+                           uint64_t *empty, unsigned &gt) {
     using namespace pair;
     const unsigned s = local / S.n_groups;
     const unsigned g = local - s * S.n_groups;
@@ -516,28 +493,18 @@ __device__ bool block_item(const Dev &d, const System &S, unsigned local, float4
     for (int c = 0; c < 6; c++) { Sum[c] = 0ull; Cmp[c] = 0ull; }
     const size_t jtp = (size_t)d.jtotal;
     const float4 *src = d.jd + (size_t)S.joff + jb;
-    constexpr unsigned TILE_BYTES = JT * sizeof(float4);
-    if (threadIdx.x == 0) {   // the first two tiles
-        tma::fence_proxy_async();
-        for (int t = 0; t < 2 && t < ntiles; t++) {
-            const unsigned b = (gt + t) & 1u;
-            tma::mbar_arrive_expect_tx(&full[b], 5 * TILE_BYTES);
-#pragma unroll
-            for (int pl = 0; pl < 5; pl++) tma::load_1d(&sj[b][pl][0], src + pl * jtp + (size_t)t * JT, TILE_BYTES, &full[b]);
-        }
-    }
+    const unsigned g0 = gt;   // the item's first tile
+    bool ok = true;
+    if (threadIdx.x == 0)     // the item's first NS tiles
+        for (int t = 0; t < (int)NS && t < ntiles && ok; t++) ok = issue_tile<JT>(sj, full, empty, g0 + t, src, jtp, t);
     const int per = JT / (int)Q;          // j per thread per tile
     const int sub = per > 64 ? 64 : per;  // j per FP32 run
-    for (int t = 0; t < ntiles; t++, gt++) {
-        const unsigned b = gt & 1u;
-        const bool ok = tma::wait_bounded(&full[b], (gt >> 1) & 1u, WAIT_LIMIT);
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) {
-                tma::drain_tiles(full, gt, ntiles - t, WAIT_LIMIT);
-                atomicOr(d.err, (unsigned)H4_ERRBIT_TIMEOUT);
-            }
-            return false;
-        }
+    int t = 0;
+    for (; t < ntiles && ok; t++) {
+        const unsigned gg = g0 + (unsigned)t, b = gg % NS;
+        const bool mine = ok && tma::wait_bounded(&full[b], (gg / NS) & 1u, WAIT_LIMIT);
+        ok = __all_sync(0xffffffffu, mine);   // warp-uniform (thread 0 also reports its refills)
+        if (!ok) break;
         for (int sb = 0; sb < per; sb += sub) {
             f2 part[6];
 #pragma unroll
@@ -553,20 +520,186 @@ __device__ bool block_item(const Dev &d, const System &S, unsigned local, float4
 #pragma unroll
             for (int c = 0; c < 6; c++) kahan2(Sum[c], Cmp[c], part[c]);
         }
-        __syncthreads();   // every thread is done with buffer b
-        if (threadIdx.x == 0 && t + 2 < ntiles) {
-            tma::fence_proxy_async();
-            tma::mbar_arrive_expect_tx(&full[b], 5 * TILE_BYTES);
-#pragma unroll
-            for (int pl = 0; pl < 5; pl++)
-                tma::load_1d(&sj[b][pl][0], src + pl * jtp + (size_t)(t + 2) * JT, TILE_BYTES, &full[b]);
-        }
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0) tma::mbar_arrive(&empty[b]);   // this warp is done with stage b
+        if (threadIdx.x == 0 && t + (int)NS < ntiles) ok = issue_tile<JT>(sj, full, empty, gg + NS, src, jtp, t + NS);
     }
+    // the block meets once per item: every warp has finished (or given up)
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+            // copies of this item possibly still in flight: tiles t .. t + NS - 1
+            for (int k = t; k < ntiles && k < t + (int)NS; k++)
+                tma::wait_bounded(&full[(g0 + k) % NS], ((g0 + k) / NS) & 1u, WAIT_LIMIT);
+            atomicOr(d.err, (unsigned)H4_ERRBIT_TIMEOUT);
+        }
+        return false;
+    }
+    gt = g0 + (unsigned)ntiles;
     double *part_s = d.part + S.part_off + (size_t)(s * Q + qq) * 6 * nact;
 #pragma unroll
     for (int c = 0; c < 6; c++) {
         if (k0 < nact) part_s[(size_t)c * nact + k0] = (double)lo2(Sum[c]) - (double)lo2(Cmp[c]);
         if (k1 < nact) part_s[(size_t)c * nact + k1] = (double)hi2(Sum[c]) - (double)hi2(Cmp[c]);
+    }
+    return true;
+}
+
+// ---- P1 (mixed form, e2 > 0): one warp item through a per-warp TMA ring ------
+// The warp item of pair::mixed_warp_item (NI = 1) or mixed_warp_item_x2
+// (NI = 2) with its j data brought into shared memory instead of loaded by
+// every lane from L2: stages of WARP_STAGE_J consecutive j (three 1-D bulk
+// copies, one per plane of jf0/jf1/jf2, issued by lane 0 and completing on
+// the stage's mbarrier), WARP_STAGES of them in flight, so the L2 latency is
+// hidden behind the pair arithmetic of the stages before.  Lane l takes the
+// stage's j l and l + 32 -- the same j in the same order as the L2 form, so
+// the sums are the same.  gw counts the stages this warp has consumed.
+// Returns false when a wait timed out (the error bit is then set).
+__device__ __forceinline__ void issue_stage(float4 (*ring)[3][WARP_STAGE_J], uint64_t *wfull, unsigned gs,
+                                            const float4 *jf0, const float4 *jf1, const float4 *jf2, int j0, int cnt) {
+    const unsigned st = gs % WARP_STAGES;
+    const unsigned bytes = (unsigned)cnt * (unsigned)sizeof(float4);
+    tma::fence_proxy_async();
+    tma::mbar_arrive_expect_tx(&wfull[st], 3 * bytes);
+    tma::load_1d(&ring[st][0][0], jf0 + j0, bytes, &wfull[st]);
+    tma::load_1d(&ring[st][1][0], jf1 + j0, bytes, &wfull[st]);
+    tma::load_1d(&ring[st][2][0], jf2 + j0, bytes, &wfull[st]);
+}
+
+template <int NI>
+__device__ bool ring_warp_item(const Dev &d, const System &S, const unsigned *move, unsigned nact, unsigned k0, int jb,
+                               int je, double *part_s, float4 (*ring)[3][WARP_STAGE_J], uint64_t *wfull, unsigned &gw,
+                               int lane) {
+    using namespace pair;
+    const float4 *jf0 = d.jf0 + S.off, *jf1 = d.jf1 + S.off, *jf2 = d.jf2 + S.off;
+    const float e2f = (float)S.e2;
+    const int nst = (je - jb + WARP_STAGE_J - 1) / WARP_STAGE_J;
+    const unsigned gs0 = gw;
+    if (lane == 0)
+        for (int k = 0; k < WARP_STAGES && k < nst; k++)
+            issue_stage(ring, wfull, gs0 + k, jf0, jf1, jf2, jb + k * WARP_STAGE_J,
+                        min(WARP_STAGE_J, je - jb - k * WARP_STAGE_J));
+    constexpr int RUN = 512 / WARP_STAGE_J;   // stages per FP32 run (16 j per lane)
+    IPair ip;
+    IParticle i1;
+    if (NI == 2)
+        ip = pack_pair(load_i(jf0, jf1, jf2, move[k0]), load_i(jf0, jf1, jf2, move[k0 + 1]));
+    else
+        i1 = load_i(jf0, jf1, jf2, move[k0]);
+    const f2 e2 = pk2(e2f, e2f), m3 = pk2(-3.0f, -3.0f);
+    f2 Sx[6], Cx[6], px[6];
+    float S1[6], C1[6], p1[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) { Sx[c] = 0ull; Cx[c] = 0ull; px[c] = 0ull; S1[c] = 0.f; C1[c] = 0.f; p1[c] = 0.f; }
+    bool ok = true;
+    int k = 0;
+    for (; k < nst; k++) {
+        const unsigned gs = gs0 + (unsigned)k, st = gs % WARP_STAGES;
+        ok = __all_sync(0xffffffffu, tma::wait_bounded(&wfull[st], (gs / WARP_STAGES) & 1u, WAIT_LIMIT));
+        if (!ok) break;
+        const int j0 = jb + k * WARP_STAGE_J;
+#pragma unroll
+        for (int h = 0; h < WARP_STAGE_J / 32; h++) {
+            const int jj = lane + 32 * h;
+            if (j0 + jj < je) {
+                const float4 a = ring[st][0][jj], b = ring[st][1][jj], c = ring[st][2][jj];
+                if (NI == 2)
+                    pair_x2(ip, pk2(a.x, a.x), pk2(a.y, a.y), pk2(a.z, a.z), pk2(a.w, a.w), pk2(b.x, b.x),
+                            pk2(b.y, b.y), pk2(b.z, b.z), pk2(c.x, c.x), pk2(c.y, c.y), pk2(c.z, c.z), e2, m3, px);
+                else
+                    pair_mixed<false>(i1, a, b, c, e2f, false, p1);
+            }
+        }
+        __syncwarp();
+        if (lane == 0 && k + WARP_STAGES < nst)
+            issue_stage(ring, wfull, gs + WARP_STAGES, jf0, jf1, jf2, j0 + WARP_STAGES * WARP_STAGE_J,
+                        min(WARP_STAGE_J, je - j0 - WARP_STAGES * WARP_STAGE_J));
+        if ((k % RUN) == RUN - 1 || k == nst - 1) {
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                if (NI == 2) { kahan2(Sx[c], Cx[c], px[c]); px[c] = 0ull; }
+                else { kahan_add(S1[c], C1[c], p1[c]); p1[c] = 0.f; }
+            }
+        }
+    }
+    if (!ok) {
+        if (lane == 0) {   // stages possibly still in flight: k .. k + WARP_STAGES - 1
+            for (int q = k; q < nst && q < k + WARP_STAGES; q++)
+                tma::wait_bounded(&wfull[(gs0 + q) % WARP_STAGES], ((gs0 + q) / WARP_STAGES) & 1u, WAIT_LIMIT);
+            atomicOr(d.err, (unsigned)H4_ERRBIT_TIMEOUT);
+        }
+        return false;
+    }
+    gw = gs0 + (unsigned)nst;
+    // Kahan pairs (value S - C) summed over the lanes in double-single FP32
+    constexpr int V = NI == 2 ? 16 : 8;
+    float h[V], l[V];
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+        if (NI == 2) {
+            h[2 * c] = lo2(Sx[c]); h[2 * c + 1] = hi2(Sx[c]);
+            l[2 * c] = -lo2(Cx[c]); l[2 * c + 1] = -hi2(Cx[c]);
+        } else {
+            h[c] = S1[c];
+            l[c] = -C1[c];
+        }
+    }
+#pragma unroll
+    for (int x = 6 * NI; x < V; x++) { h[x] = 0.f; l[x] = 0.f; }
+    rs_sum_ds<V, 16>(h, l, lane);
+    const int x = rs_index<V>(lane);
+    if (rs_first<V>(lane) && x < 6 * NI) part_s[(size_t)(x / NI) * nact + k0 + (x % NI)] = (double)h[0] + (double)l[0];
+    return true;
+}
+
+// ---- P1: one warp item of some system's force sum ---------------------------
+template <int MODE>
+__device__ bool force_item(const Dev &d, const System &S, unsigned local, int lane, float4 (*ring)[3][WARP_STAGE_J],
+                           uint64_t *wfull, unsigned &gw) {
+    const unsigned s = local / S.n_groups;
+    const unsigned g = local - s * S.n_groups;
+    const int off = S.off;
+    const int jb = (int)(s * S.chunk);
+    const int je = min(S.n, jb + (int)S.chunk);
+    const unsigned nact = S.nact;
+    double *part_s = d.part + S.part_off + (size_t)s * 6 * nact;
+    const unsigned *move = d.move + off;
+    if (MODE == H4_FORCE_EXACT) {
+        const unsigned k = g * 32 + lane;
+        const unsigned cnt = min(32u, nact - g * 32);
+        if (kBoundsCheck && !__all_sync(0xffffffffu, item_ok(d, S, s, g * 32, cnt, 0, S.n, (unsigned)lane))) return true;
+        if (k < nact) {
+            double f[6];
+            pair::exact_sum(d.pr + off, d.pv + off, S.n, move[k], S.e2, f);
+#pragma unroll
+            for (int c = 0; c < 6; c++) part_s[(size_t)c * nact + k] = f[c];
+        }
+        return true;
+    }
+    const unsigned k0 = g * S.ig;
+    const unsigned cnt = min(S.ig, nact - k0);
+    if (kBoundsCheck && !__all_sync(0xffffffffu, item_ok(d, S, s, k0, cnt, jb, je, (unsigned)lane))) return true;
+    if (MODE == H4_FORCE_FP64) {
+        const dbl4 *pr = d.pr + off, *pv = d.pv + off;
+        if (cnt == 4) {
+            pair::fp64_warp_item<4>(pr, pv, move, nact, k0, jb, je, S.e2, part_s, lane);
+        } else {
+            unsigned k = k0;
+            if (cnt >= 2) { pair::fp64_warp_item<2>(pr, pv, move, nact, k, jb, je, S.e2, part_s, lane); k += 2; }
+            if (cnt & 1) pair::fp64_warp_item<1>(pr, pv, move, nact, k, jb, je, S.e2, part_s, lane);
+        }
+    } else {
+        const float4 *a = d.jf0 + off, *b = d.jf1 + off, *c = d.jf2 + off;
+        const float e2 = (float)S.e2;
+        if (S.e2 > 0.0)   // a packed pair, or one particle, j through the warp's ring
+            return cnt == 2 ? ring_warp_item<2>(d, S, move, nact, k0, jb, je, part_s, ring, wfull, gw, lane)
+                            : ring_warp_item<1>(d, S, move, nact, k0, jb, je, part_s, ring, wfull, gw, lane);
+        {   // e2 = 0: the self term masked, j from L2
+            unsigned k = k0;
+            while (k < k0 + cnt) {
+                pair::mixed_warp_item<1, true>(a, b, c, move, nact, k, jb, je, e2, part_s, lane);
+                k++;
+            }
+        }
     }
     return true;
 }
@@ -629,9 +762,15 @@ __device__ __forceinline__ void phase_mark(const Dev &d, int phase, unsigned lon
 
 template <int MODE>
 __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, int iters, int init, int force_only) {
-    // per-system prefix sums, [nsys + 1] each: particle offsets, warp items,
-    // block items, active particles
-    extern __shared__ unsigned s_dyn[];
+    // dynamic shared memory: the mixed form's tile area (block-item j tiles,
+    // or the warps' j rings), then per-system prefix sums, [nsys + 1] each:
+    // particle offsets, warp items, block items, active particles
+    extern __shared__ __align__(128) unsigned char s_raw[];
+    constexpr size_t tile_area = MODE == H4_FORCE_MIXED ? TILE_AREA_BYTES : 0;
+    float4(*sj)[5][JT_MAX] = reinterpret_cast<float4(*)[5][JT_MAX]>(s_raw);
+    float4(*ring)[3][WARP_STAGE_J] =
+        reinterpret_cast<float4(*)[3][WARP_STAGE_J]>(s_raw + (threadIdx.x >> 5) * WARP_RING_BYTES);
+    unsigned *s_dyn = reinterpret_cast<unsigned *>(s_raw + tile_area);
     unsigned *s_off = s_dyn;
     unsigned *s_prefix = s_off + d.nsys + 1;
     unsigned *s_prefix_b = s_prefix + d.nsys + 1;
@@ -640,15 +779,19 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
     __shared__ double redd[WARPS];
     __shared__ unsigned s_item[WARPS];
     __shared__ unsigned s_bitem;
-    // j tiles of the block items (two buffers) and their barriers
-    __shared__ __align__(128) float4 sj[MODE == H4_FORCE_MIXED ? 2 : 1][5][MODE == H4_FORCE_MIXED ? JT_MAX : 1];
-    __shared__ __align__(8) uint64_t s_full[2];
+    // barriers of the block-item stages and of the warps' rings
+    __shared__ __align__(8) uint64_t s_full[NS], s_empty[NS], s_wfull[WARPS][WARP_STAGES];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     unsigned gt = 0;   // block-item tiles consumed by this block
+    unsigned gw = 0;   // warp-item stages consumed by this warp
     if (MODE == H4_FORCE_MIXED) {
         if (threadIdx.x == 0) {
-            tma::mbar_init(&s_full[0], 1);
-            tma::mbar_init(&s_full[1], 1);
+            for (unsigned b = 0; b < NS; b++) {
+                tma::mbar_init(&s_full[b], 1);
+                tma::mbar_init(&s_empty[b], WARPS);
+            }
+            for (int q = 0; q < WARPS; q++)
+                for (int st = 0; st < WARP_STAGES; st++) tma::mbar_init(&s_wfull[q][st], 1);
             tma::mbar_init_fence();
         }
         __syncthreads();
@@ -714,8 +857,8 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
                 if (item >= total_b) break;
                 const int c = find_seg(s_prefix_b, d.nsys, item);
                 const System &S = d.sys[c];
-                tiles_ok = S.jt == 128u ? block_item<128>(d, S, item - s_prefix_b[c], sj, s_full, gt)
-                                        : block_item<JT_MAX>(d, S, item - s_prefix_b[c], sj, s_full, gt);
+                tiles_ok = S.jt == 128u ? block_item<128>(d, S, item - s_prefix_b[c], sj, s_full, s_empty, gt)
+                                        : block_item<JT_MAX>(d, S, item - s_prefix_b[c], sj, s_full, s_empty, gt);
                 if (!tiles_ok) break;   // a tile wait timed out: straight to the barrier, which fails
             }
         }
@@ -727,7 +870,8 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
             __syncwarp();
             if (item >= total) break;
             const int c = find_seg(s_prefix, d.nsys, item);
-            force_item<MODE>(d, d.sys[c], item - s_prefix[c], lane);
+            if (!force_item<MODE>(d, d.sys[c], item - s_prefix[c], lane, ring, s_wfull[w], gw))
+                break;   // a stage wait timed out: straight to the barrier, which fails
         }
         if (!grid_sync(d)) return;
         phase_mark(d, 2, t_prev);
@@ -1169,7 +1313,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     if (e == cudaSuccess) e = cudaMemsetAsync(d.launches, 0, 8, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.phase_ns, 0, 32, s);
     // persistent grid: every block resident (cooperative launch)
-    E->smem = sizeof(unsigned) * 4 * (nsys + 1);
+    E->smem = (mode == H4_FORCE_MIXED ? TILE_AREA_BYTES : 0) + sizeof(unsigned) * 4 * (nsys + 1);
     int per_sm = 0;
     if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel_for(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel_for(mode), THREADS, E->smem);
