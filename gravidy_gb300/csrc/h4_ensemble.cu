@@ -398,9 +398,10 @@ __device__ __forceinline__ void predict_one(const Dev &d, const System &S, size_
     } else {
         exact::predict(S.itime, d.t[g], d.f + 6 * g, d.r[g], d.v[g], pr, pv);
     }
-    d.pr[g] = pr;
-    d.pv[g] = pv;
-    if (MODE == H4_FORCE_MIXED) {
+    if (MODE != H4_FORCE_MIXED) {   // the mixed corrector recomputes its particles' predictors
+        d.pr[g] = pr;
+        d.pv[g] = pv;
+    } else {
         float4 a, b, cc;
         exact::pack_jf(pr, pv, a, b, cc);
         d.jf0[g] = a;
@@ -718,6 +719,7 @@ __device__ __forceinline__ bool correct_ok(const Dev &d, const System &S, unsign
 }
 
 // fn: the sum of the particle's partial forces (exact::sum_partials_*).
+template <int MODE>
 __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k, bool init, const double fn[6]) {
     const unsigned i = d.move[S.off + k];
     const size_t g = (size_t)S.off + i;
@@ -735,7 +737,14 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
     for (int q = 0; q < 6; q++) { o[q] = fp[q]; op[q] = o[q]; fp[q] = fn[q]; }
     dbl4 r = d.r[g], v = d.v[g];
     double a2[3], a3[3], ndt;
-    const bool ok = exact::correct(S.itime, S.eta, S.dt_min, S.dt_max, fn, o, d.pr[g], d.pv[g], d.dt[g], r, v, a2,
+    dbl4 pr, pv;
+    if (MODE == H4_FORCE_MIXED) {   // phase B's predictor of this particle, from the same inputs
+        predict_fma(S.itime, d.t[g], o, r, v, pr, pv);
+    } else {
+        pr = d.pr[g];
+        pv = d.pv[g];
+    }
+    const bool ok = exact::correct(S.itime, S.eta, S.dt_min, S.dt_max, fn, o, pr, pv, d.dt[g], r, v, a2,
                                    a3, ndt);
     d.r[g] = r;
     d.v[g] = v;
@@ -886,7 +895,7 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
             if (!exact::warp_reduce(S.split) || !__all_sync(0xffffffffu, correct_ok(d, S, k))) continue;
             double fn[6];
             exact::sum_partials_warp(d.part + S.part_off, S.nact, k, S.split, lane, fn);
-            if (lane == 0) correct_one(d, S, k, init != 0, fn);
+            if (lane == 0) correct_one<MODE>(d, S, k, init != 0, fn);
         }
         for (unsigned a = gtid; a < c_a; a += nthreads) {
             const int c = find_seg(s_act, d.nsys, a);
@@ -895,7 +904,7 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
             if (exact::warp_reduce(S.split) || !correct_ok(d, S, k)) continue;
             double fn[6];
             exact::sum_partials_thread(d.part + S.part_off, S.nact, k, S.split, fn);
-            correct_one(d, S, k, init != 0, fn);
+            correct_one<MODE>(d, S, k, init != 0, fn);
         }
         if (!grid_sync(d)) return;
         phase_mark(d, 3, t_prev);

@@ -24,12 +24,57 @@ constexpr int ITEMS_PER_WARP = 12;
 #endif
 constexpr bool kFp64SmallSplit = H4_FP64_SMALL_SPLIT != 0;
 
-// Warp `warp` (lane `lane`) of `nwarps` takes work items from the queue in
-// the control block until it is empty.  The j-split is fixed by nact, n and
-// `split_warps` (the warp count the split is sized for: enough items for
-// every warp to take several, chunks of at least 64 j, partial sums within
-// the scratch), not by the warps that actually run, so any launch shape gives
-// the same items.  first: this caller publishes the split.
+// The queue loop for items of G particles (G a compile-time constant, so
+// the common all-IG shape keeps fully unrolled items).
+template <int G>
+__device__ __forceinline__ void items_loop(const H4Dev &d, unsigned nact, unsigned n_groups, unsigned total, int chunk,
+                                           int lane) {
+    for (;;) {
+        unsigned item;
+        if (lane == 0) item = atomicAdd(&d.ctrl->work_next, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        const unsigned s = item / n_groups;
+        const unsigned g = item - s * n_groups;
+        const int j_begin = (int)s * chunk;
+        const int j_end = min(d.n, j_begin + chunk);
+        const unsigned k0 = g * G;
+        const unsigned cnt = min((unsigned)G, nact - k0);
+        double *part_s = d.part + (size_t)s * 6 * nact;
+        if (kBoundsCheck && !pair::warp_item_ok(d, nact, k0, cnt, j_begin, j_end, s, lane, BS_FP64_J)) continue;
+        if (cnt == (unsigned)G) {
+            pair::fp64_warp_item<G>(d.pr, d.pv, d.move, nact, k0, j_begin, j_end, d.e2, part_s, lane);
+        } else {
+            unsigned k = k0, left = cnt;
+            if (G > 4 && left >= 4) {
+                pair::fp64_warp_item<4>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
+                k += 4; left -= 4;
+            }
+            if (G > 2 && left >= 2) {
+                pair::fp64_warp_item<2>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
+                k += 2; left -= 2;
+            }
+            if (left & 1) pair::fp64_warp_item<1>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
+        }
+    }
+}
+
+// Small steps' items (1 or 2 particles), out of line so that the common
+// shape's loop keeps its register allocation.
+static __device__ __noinline__ void small_items(const H4Dev &d, unsigned nact, unsigned n_groups, unsigned total, int chunk,
+                                         int lane, unsigned ig) {
+    if (ig >= 2)
+        items_loop<2>(d, nact, n_groups, total, chunk, lane);
+    else
+        items_loop<1>(d, nact, n_groups, total, chunk, lane);
+}
+
+// Warp lane `lane` takes work items from the queue in the control block
+// until it is empty.  The j-split is fixed by nact, n and `split_warps` (the
+// warp count the split is sized for: enough items for every warp to take
+// several, chunks of at least 64 j, partial sums within the scratch), not by
+// the warps that actually run, so any launch shape gives the same items.
+// first: this caller publishes the split.
 __device__ __forceinline__ void force_items(const H4Dev &d, unsigned split_warps, int lane, bool first) {
     const unsigned nact = d.ctrl->nact;
     if (nact == 0) return;
@@ -57,34 +102,10 @@ __device__ __forceinline__ void force_items(const H4Dev &d, unsigned split_warps
         d.ctrl->force_split = split;
         d.ctrl->work_total = total;
     }
-    for (;;) {
-        unsigned item;
-        if (lane == 0) item = atomicAdd(&d.ctrl->work_next, 1u);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= total) break;
-        const unsigned s = item / n_groups;
-        const unsigned g = item - s * n_groups;
-        const int j_begin = (int)s * chunk;
-        const int j_end = min(d.n, j_begin + chunk);
-        const unsigned k0 = g * ig;
-        const unsigned cnt = min(ig, nact - k0);
-        double *part_s = d.part + (size_t)s * 6 * nact;
-        if (kBoundsCheck && !pair::warp_item_ok(d, nact, k0, cnt, j_begin, j_end, s, lane, BS_FP64_J)) continue;
-        if (cnt == (unsigned)IG) {
-            pair::fp64_warp_item<IG>(d.pr, d.pv, d.move, nact, k0, j_begin, j_end, d.e2, part_s, lane);
-        } else {
-            unsigned k = k0, left = cnt;
-            if (IG > 4 && left >= 4) {
-                pair::fp64_warp_item<4>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
-                k += 4; left -= 4;
-            }
-            if (left >= 2) {
-                pair::fp64_warp_item<2>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
-                k += 2; left -= 2;
-            }
-            if (left & 1) pair::fp64_warp_item<1>(d.pr, d.pv, d.move, nact, k, j_begin, j_end, d.e2, part_s, lane);
-        }
-    }
+    if (ig == (unsigned)IG)
+        items_loop<IG>(d, nact, n_groups, total, chunk, lane);
+    else
+        small_items(d, nact, n_groups, total, chunk, lane, ig);
 }
 
 // Bit-identical restatement of Hermite4CPU::update_acc_jrk for active
