@@ -69,7 +69,7 @@ def mixed_candidates(n: int, a: int):
     out = []
     if a >= 5:      # 256 and more active: block-tiled items, wide to narrow
         for bti in (512, 256, 128, 64):
-            for chunk in (1024, 2048, 4096):
+            for chunk in (512, 1024, 2048, 4096):
                 out.append((bti, chunk, 256))
         out += [(512, 1024, 128), (256, 1024, 128)]
         out += [(2, 2048, 256), (2, 4096, 256)]

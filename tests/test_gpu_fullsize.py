@@ -1,9 +1,9 @@
 """Parity at the benchmark sizes, through properties that do not need a full
 O(N^2) CPU reference:
 
-  * N = 2^20 (C5) and N = 65536 (C2): acc/jerk of a sample of particles
+  * N = 2^20 (C5) and N = 65536 (C2): acc/jerk of 512 sampled particles
     against the oracle's per-particle sums (the oracle does only the sampled
-    rows, O(sample * N));
+    rows, O(sample * N)), FP64 within 1e-12 and mixed within 1e-4;
   * momentum balance of the all-active force sum: sum_i m_i a_i and
     sum_i m_i a1_i vanish to rounding (Newton's third law), relative to
     sum_i m_i |a_i|;
@@ -24,7 +24,7 @@ def test_sampled_forces_at_full_size(n, imf, soft):
     m, p, v = ics.plummer(n, 5, imf)
     ns = NbodySystem(m, p, v, softening=soft)
     rng = np.random.default_rng(n)
-    move = np.sort(rng.choice(n, size=48, replace=False)).astype(np.uint32)
+    move = np.sort(rng.choice(n, size=512, replace=False)).astype(np.uint32)
     pr = np.zeros((n, 4)); pr[:, :3] = p; pr[:, 3] = ns.mass
     pv = np.zeros((n, 4)); pv[:, :3] = v
     want = orc.forces_for(orc.make_predictors(ns.mass, p, v), ns.e2, move)
@@ -32,7 +32,7 @@ def test_sampled_forces_at_full_size(n, imf, soft):
         with Hermite4GPU(ns, mode=mode) as g:
             got = g.forces_for(pr, pv, move)
         assert rel_err_vec(got[:, :3], want[:, :3]).max() < tol, mode
-        assert rel_err_vec(got[:, 3:], want[:, 3:]).max() < tol * (1 if mode == "fp64" else 10), mode
+        assert rel_err_vec(got[:, 3:], want[:, 3:]).max() < tol, mode
 
 
 @pytest.mark.parametrize("n", [65536, 1 << 18])
