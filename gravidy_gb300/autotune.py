@@ -27,9 +27,9 @@ so a probe suffices -- for every bucket a homogeneous ensemble of that N
 (about 2^20 particles, equal-mass and Salpeter systems alternating) with the
 bucket's active count forced on every system (h4_ens_tune_force).
 
-Ties go, deterministically, to the first candidate within TIE of the fastest
-(the current choice first in the descent), so that a re-run reproduces the
-table.  Finally C4 runs (to t = 1 mixed, 0.125 FP64) with the default and the
+Ties go, deterministically, to the first candidate within TIE (descent) or
+PROBE_TIE (probes) of the fastest -- the current choice first in the descent
+-- so that a re-run reproduces the table.  Finally C4 runs (to t = 1 mixed, 0.125 FP64) with the default and the
 tuned table and both device times are recorded.
 
     python -m gravidy_gb300.autotune --out gravidy_gb300/tuning/ensemble_gb300.json
@@ -48,7 +48,8 @@ from .ensemble import NB_A, NB_N, Ensemble
 N_REP = [512, 1024, 2048, 4096, 8192, 16384]
 A_LO = [1, 2, 4, 16, 64, 256, 1024, 4096]          # first active count of each bucket
 A_REP = [1, 3, 12, 48, 192, 768, 3072, 8192]       # count used where C4 gives none
-TIE = 0.01
+TIE = 0.01            # the mixed descent: repeatable whole-C4 timings
+PROBE_TIE = 0.03      # the FP64 probes: single short launches, noisier
 CHUNKS = [64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384]
 
 
@@ -175,6 +176,44 @@ def tune_mixed(verbose: bool = True) -> dict:
                   f"(best {best:.4f}, current was {times[0]:.4f})", flush=True)
     table.update({"c4_steps": steps.astype(int).tolist(), "c4_interactions": inter.tolist(),
                   "eval_t": EVAL_T, "descent": trace})
+    return table
+
+
+def tune(mode: str = "fp64", total_particles: int = 1 << 20, reps: int = 3, verbose: bool = True) -> dict:
+    """FP64 probe tuning: per N bucket a homogeneous ensemble of about
+    total_particles particles; per active bucket every candidate timed with
+    the bucket's C4 active count forced on every system (best of reps)."""
+    steps, inter = record_mixture(mode, t_end=RECORD_T[mode], verbose=verbose)
+    ig_tab = np.zeros((NB_N, NB_A), dtype=int)
+    ch_tab = np.zeros((NB_N, NB_A), dtype=int)
+    jt_tab = np.full((NB_N, NB_A), 256, dtype=int)
+    rate_tab = np.zeros((NB_N, NB_A))
+    nact_tab = np.zeros((NB_N, NB_A), dtype=int)
+    for b, n in enumerate(N_REP):
+        E, k = probe_ensemble(mode, n, total_particles)
+        with E:
+            for a in range(NB_A):
+                if steps[b, a] > 0:   # interaction-weighted mean active count of the bucket
+                    nact = int(round(inter[b, a] / steps[b, a] / n))
+                    nact = max(A_LO[a], min(nact, (A_LO[a + 1] - 1) if a + 1 < NB_A else nact))
+                else:
+                    nact = A_REP[a]
+                nact = max(1, min(nact, n))
+                nact_tab[b, a] = nact
+                cands = candidates(mode, n, nact)
+                times = [time_candidate(E, nact, c, reps) for c in cands]
+                best = min(times)
+                pick = next(i for i, t in enumerate(times) if t <= best * (1.0 + PROBE_TIE))
+                ig, chunk, jt = cands[pick]
+                ig_tab[b, a], ch_tab[b, a], jt_tab[b, a] = ig, chunk, jt
+                rate_tab[b, a] = k * nact * n / (times[pick] * 1e-3)
+                if verbose:
+                    print(f"{mode} N={n:6d} nact={nact:6d} systems={k:4d} weight={inter[b, a]:.2e}: ig={ig} "
+                          f"chunk={chunk:6d} jtile={jt} {times[pick]:8.4f} ms (best {best:8.4f}) "
+                          f"{rate_tab[b, a]:.3e} int/s", flush=True)
+    table = {"ig": ig_tab.tolist(), "chunk": ch_tab.tolist(), "jtile": jt_tab.tolist(),
+             "interactions_per_s": rate_tab.tolist(), "n_rep": N_REP, "nact_probe": nact_tab.tolist(),
+             "c4_steps": steps.astype(int).tolist(), "c4_interactions": inter.tolist()}
     return table
 
 
