@@ -100,6 +100,7 @@ struct Dev {
     System *sys;
     dbl4 *r, *v, *pr, *pv;
     double *f, *old, *a2, *a3, *t, *dt;
+    double *tn;                  // t + dt of every particle (exact::add), set by the corrector
     float4 *jf0, *jf1, *jf2;
     float4 *jd;                  // [5][jtotal] duplicated j data of the block-tiled items, each system's
                                  // at joff, padded to npad with zero-mass far-away particles
@@ -244,18 +245,26 @@ __device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *re
             if (threadIdx.x == 0) { S.items = 0; S.bitems = 0; S.nact = 0; }
             return;
         }
-        // Hermite4::next_integration_time (Hermite4.cpp:90-102) for this system
-        double m = __longlong_as_double((long long)exact::INF_BITS);
-        for (int i = threadIdx.x; i < n; i += THREADS) m = fmin(m, exact::add(d.t[off + i], d.dt[off + i]));
+        // Hermite4::next_integration_time (Hermite4.cpp:90-102) for this
+        // system: the least t + dt, as the least bit pattern of the stored
+        // tn (t + dt > 0; a NaN pattern sorts above +inf, as fmin ignores
+        // NaN) -- integer work, where FP64 adds and minima on one SM would
+        // take longer than the rest of the phase
+        const unsigned long long *tnb = reinterpret_cast<const unsigned long long *>(d.tn + off);
+        unsigned long long mb = exact::INF_BITS;
+#pragma unroll 4
+        for (int i = threadIdx.x; i < n; i += THREADS) mb = min(mb, tnb[i]);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, o));
+        for (int o = 16; o > 0; o >>= 1) mb = min(mb, __shfl_down_sync(0xffffffffu, mb, o));
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        unsigned long long *redb = reinterpret_cast<unsigned long long *>(redd);
         __syncthreads();
-        if (lane == 0) redd[w] = m;
+        if (lane == 0) redb[w] = mb;
         __syncthreads();
-        m = redd[0];
-        for (int k = 1; k < WARPS; k++) m = fmin(m, redd[k]);
+        mb = redb[0];
+        for (int k = 1; k < WARPS; k++) mb = min(mb, redb[k]);
         __syncthreads();
+        const double m = exact::bits_to_double(mb);
         // the reference's loop condition, on the last step's block time
         const bool stop = S.err != 0u || !(S.itime < S.t_end);
         if (stop) {
@@ -263,6 +272,10 @@ __device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *re
             return;
         }
         itime = m;
+        // Hermite4::find_particles_to_move (Hermite4.cpp:64-88): the test
+        // |itime - tn| < 2^-51 as a window of bit patterns
+        unsigned long long wlo = 0, whi = 0;
+        const bool window = exact::active_window(itime, wlo, whi);
         // ascending compaction, 8 particles per thread per round
         for (int base = 0; base < n; base += THREADS * 8) {
             unsigned flags = 0, cnt = 0;
@@ -270,7 +283,7 @@ __device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *re
 #pragma unroll
             for (int q = 0; q < 8; q++) {
                 const int i = i0 + q;
-                if (i < n && exact::is_active(itime, d.t[off + i], d.dt[off + i])) {
+                if (i < n && (window ? tnb[i] - wlo <= whi - wlo : exact::is_active_tn(itime, d.tn[off + i]))) {
                     flags |= 1u << q;
                     cnt++;
                 }
@@ -727,8 +740,10 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
     if (init) {
 #pragma unroll
         for (int q = 0; q < 6; q++) fp[q] = fn[q];
-        d.dt[g] = exact::init_dt(fn, (double)0.01f, S.dt_min, S.dt_max);
+        const double dt0 = exact::init_dt(fn, (double)0.01f, S.dt_min, S.dt_max);
+        d.dt[g] = dt0;
         d.t[g] = 0.0;
+        d.tn[g] = exact::add(0.0, dt0);
         return;
     }
     double o[6];
@@ -752,6 +767,7 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
     for (int q = 0; q < 3; q++) { d.a2[3 * g + q] = a2[q]; d.a3[3 * g + q] = a3[q]; }
     d.t[g] = S.itime;
     d.dt[g] = ndt;
+    d.tn[g] = exact::add(S.itime, ndt);
     if (!ok) {
         atomicOr(&S.err, (unsigned)H4_ERRBIT_NONFINITE);
         atomicOr(d.err, (unsigned)H4_ERRBIT_NONFINITE);
@@ -773,7 +789,8 @@ template <int MODE>
 __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, int iters, int init, int force_only) {
     // dynamic shared memory: the mixed form's tile area (block-item j tiles,
     // or the warps' j rings), then per-system prefix sums, [nsys + 1] each:
-    // particle offsets, warp items, block items, active particles
+    // particle offsets, warp items, block items, and the active particles of
+    // the systems whose partials a warp per particle reduces, and of the rest
     extern __shared__ __align__(128) unsigned char s_raw[];
     constexpr size_t tile_area = MODE == H4_FORCE_MIXED ? TILE_AREA_BYTES : 0;
     float4(*sj)[5][JT_MAX] = reinterpret_cast<float4(*)[5][JT_MAX]>(s_raw);
@@ -783,7 +800,8 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
     unsigned *s_off = s_dyn;
     unsigned *s_prefix = s_off + d.nsys + 1;
     unsigned *s_prefix_b = s_prefix + d.nsys + 1;
-    unsigned *s_act = s_prefix_b + d.nsys + 1;
+    unsigned *s_actw = s_prefix_b + d.nsys + 1;
+    unsigned *s_actt = s_actw + d.nsys + 1;
     __shared__ unsigned red[WARPS];
     __shared__ double redd[WARPS];
     __shared__ unsigned s_item[WARPS];
@@ -820,7 +838,7 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
         if (!grid_sync(d)) return;
         phase_mark(d, 0, t_prev);
         // prefix sums of the systems' counts
-        unsigned c_off = 0, c_w = 0, c_b = 0, c_a = 0;
+        unsigned c_off = 0, c_w = 0, c_b = 0, c_aw = 0, c_at = 0;
         for (int base = 0; base < d.nsys; base += THREADS) {
             const int c = base + threadIdx.x;
             const bool v = c < d.nsys;
@@ -828,21 +846,25 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
             const unsigned x_w = v ? d.sys[c].items : 0u;
             const unsigned x_b = v ? d.sys[c].bitems : 0u;
             const unsigned x_a = v ? d.sys[c].nact : 0u;
-            unsigned t0, t1, t2, t3;
+            const unsigned x_aw = (v && exact::warp_reduce(d.sys[c].split)) ? x_a : 0u;
+            unsigned t0, t1, t2, t3, t4;
             const unsigned e0 = block_scan_u(x_off, red, &t0);
             const unsigned e1 = block_scan_u(x_w, red, &t1);
             const unsigned e2 = block_scan_u(x_b, red, &t2);
-            const unsigned e3 = block_scan_u(x_a, red, &t3);
+            const unsigned e3 = block_scan_u(x_aw, red, &t3);
+            const unsigned e4 = block_scan_u(x_a - x_aw, red, &t4);
             if (v) {
                 s_off[c] = c_off + e0;
                 s_prefix[c] = c_w + e1;
                 s_prefix_b[c] = c_b + e2;
-                s_act[c] = c_a + e3;
+                s_actw[c] = c_aw + e3;
+                s_actt[c] = c_at + e4;
             }
-            c_off += t0; c_w += t1; c_b += t2; c_a += t3;
+            c_off += t0; c_w += t1; c_b += t2; c_aw += t3; c_at += t4;
         }
         if (threadIdx.x == 0) {
-            s_off[d.nsys] = c_off; s_prefix[d.nsys] = c_w; s_prefix_b[d.nsys] = c_b; s_act[d.nsys] = c_a;
+            s_off[d.nsys] = c_off; s_prefix[d.nsys] = c_w; s_prefix_b[d.nsys] = c_b;
+            s_actw[d.nsys] = c_aw; s_actt[d.nsys] = c_at;
         }
         __syncthreads();
         // B: predictor of every particle of the systems taking a step
@@ -888,20 +910,20 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
         // D: corrector of every active particle; the partial forces of
         // systems with many j-chunks are summed by a warp per particle
         // (lane 0 corrects), the others by a thread per particle
-        for (unsigned a = gtid >> 5; a < c_a; a += nthreads >> 5) {
-            const int c = find_seg(s_act, d.nsys, a);
+        for (unsigned a = gtid >> 5; a < c_aw; a += nthreads >> 5) {
+            const int c = find_seg(s_actw, d.nsys, a);
             System &S = d.sys[c];
-            const unsigned k = a - s_act[c];
-            if (!exact::warp_reduce(S.split) || !__all_sync(0xffffffffu, correct_ok(d, S, k))) continue;
+            const unsigned k = a - s_actw[c];
+            if (!__all_sync(0xffffffffu, correct_ok(d, S, k))) continue;
             double fn[6];
             exact::sum_partials_warp(d.part + S.part_off, S.nact, k, S.split, lane, fn);
             if (lane == 0) correct_one<MODE>(d, S, k, init != 0, fn);
         }
-        for (unsigned a = gtid; a < c_a; a += nthreads) {
-            const int c = find_seg(s_act, d.nsys, a);
+        for (unsigned a = gtid; a < c_at; a += nthreads) {
+            const int c = find_seg(s_actt, d.nsys, a);
             System &S = d.sys[c];
-            const unsigned k = a - s_act[c];
-            if (exact::warp_reduce(S.split) || !correct_ok(d, S, k)) continue;
+            const unsigned k = a - s_actt[c];
+            if (!correct_ok(d, S, k)) continue;
             double fn[6];
             exact::sum_partials_thread(d.part + S.part_off, S.nact, k, S.split, fn);
             correct_one<MODE>(d, S, k, init != 0, fn);
@@ -1281,7 +1303,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     EA(d.sys, nsys); EA(d.r, total); EA(d.v, total); EA(d.pr, total); EA(d.pv, total);
     EA(d.f, 6 * total); EA(d.old, 6 * total); EA(d.a2, 3 * total); EA(d.a3, 3 * total);
     d.part_total = part_total;
-    EA(d.t, total); EA(d.dt, total); EA(d.move, total); EA(d.part, part_total);
+    EA(d.t, total); EA(d.dt, total); EA(d.tn, total); EA(d.move, total); EA(d.part, part_total);
     EA(d.queue, 1); EA(d.queue_b, 1); EA(d.bar_count, 1); EA(d.bar_gen, 1); EA(d.err, 2);
     EA(d.tune_ig, NB_N * NB_A); EA(d.tune_chunk, NB_N * NB_A); EA(d.tune_jt, NB_N * NB_A);
     EA(d.bucket, 2 * NB_N * NB_A); EA(d.forced_nact, 1); EA(d.launches, 1);
@@ -1310,9 +1332,9 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
         k_ens_pad_jd<<<std::min(nsys, 4096u), THREADS, 0, s>>>(d);
         e = cudaGetLastError();
     }
-    void *zero[] = {d.f, d.old, d.a2, d.a3, d.t, d.dt};
-    size_t zb[] = {48 * total, 48 * total, 24 * total, 24 * total, 8 * total, 8 * total};
-    for (int k = 0; k < 6 && e == cudaSuccess; k++) e = cudaMemsetAsync(zero[k], 0, zb[k], s);
+    void *zero[] = {d.f, d.old, d.a2, d.a3, d.t, d.dt, d.tn};
+    size_t zb[] = {48 * total, 48 * total, 24 * total, 24 * total, 8 * total, 8 * total, 8 * total};
+    for (int k = 0; k < 7 && e == cudaSuccess; k++) e = cudaMemsetAsync(zero[k], 0, zb[k], s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.queue, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.queue_b, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.bar_count, 0, 4, s);
@@ -1322,7 +1344,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     if (e == cudaSuccess) e = cudaMemsetAsync(d.launches, 0, 8, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.phase_ns, 0, 32, s);
     // persistent grid: every block resident (cooperative launch)
-    E->smem = (mode == H4_FORCE_MIXED ? TILE_AREA_BYTES : 0) + sizeof(unsigned) * 4 * (nsys + 1);
+    E->smem = (mode == H4_FORCE_MIXED ? TILE_AREA_BYTES : 0) + sizeof(unsigned) * 5 * (nsys + 1);
     int per_sm = 0;
     if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel_for(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel_for(mode), THREADS, E->smem);

@@ -27,8 +27,29 @@ __device__ __forceinline__ double magnitude(double x, double y, double z) {
 }
 
 // Hermite4::find_particles_to_move test (Hermite4.cpp:74-76)
+constexpr double ACTIVE_EPS = 4.440892098500626e-16;   // 2^-51
 __device__ __forceinline__ bool is_active(double itime, double t, double dt) {
-    return fabs(sub(itime, add(t, dt))) < 4.440892098500626e-16;
+    return fabs(sub(itime, add(t, dt))) < ACTIVE_EPS;
+}
+// The same test on a stored tn = add(t, dt).
+__device__ __forceinline__ bool is_active_tn(double itime, double tn) { return fabs(sub(itime, tn)) < ACTIVE_EPS; }
+
+// The bit patterns [lo, hi] of exactly the doubles tn that pass
+// is_active_tn(itime, tn), for 2^-48 <= itime < inf (returns false
+// otherwise; callers then test each tn).  A tn within 2^-51 of such an itime
+// lies in [itime / 2, 2 itime], where itime - tn is exact (Sterbenz), so the
+// test is the real inequality |itime - tn| < 2^-51; any other tn misses by
+// far more than a rounding.  Positive doubles order like their bit patterns,
+// and no non-positive or NaN pattern falls in [lo, hi].
+__device__ __forceinline__ bool active_window(double itime, unsigned long long &lo, unsigned long long &hi) {
+    if (!(itime >= 0x1p-48 && itime < bits_to_double(INF_BITS))) return false;
+    unsigned long long a = double_to_bits(__dadd_ru(itime, -ACTIVE_EPS));
+    if (__dadd_rd(itime, -ACTIVE_EPS) == bits_to_double(a)) a++;   // itime - 2^-51 itself fails the test
+    unsigned long long b = double_to_bits(__dadd_rd(itime, ACTIVE_EPS));
+    if (__dadd_ru(itime, ACTIVE_EPS) == bits_to_double(b)) b--;
+    lo = a;
+    hi = b;
+    return true;
 }
 
 // Hermite4CPU::predicted_pos_vel (Hermite4CPU.cpp:344-362) for one particle.
