@@ -12,25 +12,21 @@ The tuning follows the workload's mixture: the C4 ensemble (256 Plummer
 systems, N log-uniform in [512, 16384], half equal-mass, half Salpeter).  It
 is first integrated for a short time with the default table, and the
 library's per-bucket statistics (h4_ens_bucket_stats: block steps and
-interactions per bucket) give each bucket's weight and its typical active
-count (interaction-weighted mean).
+interactions per bucket) give each bucket's weight.
 
-Mixed form: the shape of an item decides how many items one block step
-yields, and in the ensemble only the systems that step in the same iteration
-share the GPU -- a step of one large system must still fill 152 SMs.  A probe
-of many identical systems cannot see that, so the mixed table is tuned on the
+The shape of an item decides how many items one block step yields, and in
+the ensemble only the systems that step in the same iteration share the GPU
+-- a step of one large system must still fill 152 SMs.  A probe of many
+identical systems stepping together cannot see that (it favours one j-chunk
+per system, which starves the GPU in C4), so both tables are tuned on the
 mixture itself: coordinate descent over the buckets that carry at least
 MIN_WEIGHT of the interactions, heaviest first, each candidate timed as the
 device time of the C4 ensemble from t = 0 to EVAL_T (the same block steps
-every time).  FP64 form: the FP64 warp items are small and FP64-pipe bound,
-so a probe suffices -- for every bucket a homogeneous ensemble of that N
-(about 2^20 particles, equal-mass and Salpeter systems alternating) with the
-bucket's active count forced on every system (h4_ens_tune_force).
-
-Ties go, deterministically, to the first candidate within TIE (descent) or
-PROBE_TIE (probes) of the fastest -- the current choice first in the descent
--- so that a re-run reproduces the table.  Finally C4 runs (to t = 1 mixed, 0.125 FP64) with the default and the
-tuned table and both device times are recorded.
+every time, repeatable to well under 1 %).  Ties within TIE go to the current
+choice, then to the earlier candidate, so that a re-run reproduces the
+table.  Finally C4 runs to VALIDATE_T with the default and the tuned table;
+a tuned table that does not beat the default by TIE is replaced by the
+default, and both device times are recorded.
 
     python -m gravidy_gb300.autotune --out gravidy_gb300/tuning/ensemble_gb300.json
 """
@@ -47,20 +43,20 @@ from .ensemble import NB_A, NB_N, Ensemble
 
 N_REP = [512, 1024, 2048, 4096, 8192, 16384]
 A_LO = [1, 2, 4, 16, 64, 256, 1024, 4096]          # first active count of each bucket
-A_REP = [1, 3, 12, 48, 192, 768, 3072, 8192]       # count used where C4 gives none
-TIE = 0.01            # the mixed descent: repeatable whole-C4 timings
-PROBE_TIE = 0.03      # the FP64 probes: single short launches, noisier
-CHUNKS = [64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384]
+TIE = 0.01
 
 
-def candidates(mode: str, n: int, nact: int):
-    """(ig, chunk, jtile) candidates of the FP64 probe tuning, in preference
-    order (ties go to the first)."""
+def fp64_candidates(n: int, a: int, chunk: int):
+    """(ig, chunk, jtile) candidates of the FP64 descent for N bucket n and
+    active bucket a around the current chunk: 4 or 2 particles per warp item
+    x chunk / 4 ... 4 chunk."""
     out = []
-    for ig in (4, 2, 1):
-        for chunk in reversed(CHUNKS):
-            if chunk <= 2 * n:
-                out.append((ig, chunk, 256))
+    base = min(chunk, 2 * n)
+    for ig in (4, 2):
+        for f in (1, 2, 0.5, 4, 0.25):
+            c = int(base * f)
+            if 64 <= c <= 2 * n and c % 32 == 0 and (ig, c, 256) not in out:
+                out.append((ig, c, 256))
     return out
 
 
@@ -101,29 +97,13 @@ def record_mixture(mode: str, t_end: float = 0.25, verbose: bool = True):
     return steps.astype(np.float64), inter.astype(np.float64)
 
 
-def probe_ensemble(mode: str, n: int, total_particles: int):
-    k = max(1, min(256, total_particles // n))
-    systems = []
-    for s in range(k):
-        m, p, v = ics.plummer(n, 10_000 + s, "equal" if s % 2 == 0 else "salpeter", exact_scaling_max_n=0)
-        systems.append((m, p, v, 0.01, 0.01))
-    return Ensemble(systems, mode=mode, tuning=None), k
-
-
-def time_candidate(E, nact, cand, reps):
-    ig, chunk, jt = cand
-    t = E.tune_force(nact, ig, chunk, jt)
-    if t < 50.0:   # repeat the short probes, keep the best
-        t = min([t] + [E.tune_force(nact, ig, chunk, jt) for _ in range(reps - 1)])
-    return t
-
-
 # C4 run lengths: the mixture record, the descent's objective and the
-# validation (the FP64 form runs about 22x longer than the mixed form)
+# validation (the FP64 form runs about 27x longer than the mixed form)
 RECORD_T = {"mixed": 0.25, "fp64": 0.0625}
+EVAL_T = {"mixed": 0.125, "fp64": 0.03125}
 VALIDATE_T = {"mixed": 1.0, "fp64": 0.125}
-EVAL_T = 0.125        # the mixed descent: one cycle of the largest block timestep
-MIN_WEIGHT = 0.005    # buckets carrying less of the interactions keep the default
+# buckets carrying less of the interactions keep the default
+MIN_WEIGHT = {"mixed": 0.005, "fp64": 0.02}
 
 
 def default_table(mode: str) -> dict:
@@ -143,20 +123,22 @@ def c4_seconds(mode: str, systems, table: dict, t_end: float) -> float:
     return ms * 1e-3
 
 
-def tune_mixed(verbose: bool = True) -> dict:
-    steps, inter = record_mixture("mixed", t_end=RECORD_T["mixed"], verbose=verbose)
+def tune_descent(mode: str, verbose: bool = True) -> dict:
+    steps, inter = record_mixture(mode, t_end=RECORD_T[mode], verbose=verbose)
     systems = workloads.c4_systems(256, seed=4)
-    table = default_table("mixed")
-    t_best = c4_seconds("mixed", systems, table, EVAL_T)
+    table = default_table(mode)
+    t_eval = EVAL_T[mode]
+    t_best = c4_seconds(mode, systems, table, t_eval)
     if verbose:
-        print(f"mixed: default table, C4 to t={EVAL_T}: {t_best:.4f} s", flush=True)
+        print(f"{mode}: default table, C4 to t={t_eval}: {t_best:.4f} s", flush=True)
     order = sorted(((inter[b, a], b, a) for b in range(NB_N) for a in range(NB_A)), reverse=True)
     trace = []
     for w, b, a in order:
-        if w < MIN_WEIGHT * inter.sum():
+        if w < MIN_WEIGHT[mode] * inter.sum():
             break
         cur = (table["ig"][b][a], table["chunk"][b][a], table["jtile"][b][a])
-        cands = [cur] + [c for c in mixed_candidates(N_REP[b], a) if c != cur]
+        pool = mixed_candidates(N_REP[b], a) if mode == "mixed" else fp64_candidates(N_REP[b], a, cur[1])
+        cands = [cur] + [c for c in pool if c != cur]
         times = []
         for c in cands:
             if c == cur:
@@ -164,7 +146,7 @@ def tune_mixed(verbose: bool = True) -> dict:
                 continue
             trial = json.loads(json.dumps(table))
             trial["ig"][b][a], trial["chunk"][b][a], trial["jtile"][b][a] = c
-            times.append(c4_seconds("mixed", systems, trial, EVAL_T))
+            times.append(c4_seconds(mode, systems, trial, t_eval))
         best = min(times)
         pick = next(i for i, t in enumerate(times) if t <= best * (1.0 + TIE))
         table["ig"][b][a], table["chunk"][b][a], table["jtile"][b][a] = cands[pick]
@@ -172,48 +154,10 @@ def tune_mixed(verbose: bool = True) -> dict:
         trace.append({"bucket": [b, a], "weight": float(w), "candidates": [list(c) for c in cands],
                       "seconds": times, "pick": list(cands[pick])})
         if verbose:
-            print(f"mixed N<={N_REP[b]:6d} a={a} weight={w:.2e}: pick {cands[pick]} {t_best:.4f} s "
+            print(f"{mode} N<={N_REP[b]:6d} a={a} weight={w:.2e}: pick {cands[pick]} {t_best:.4f} s "
                   f"(best {best:.4f}, current was {times[0]:.4f})", flush=True)
     table.update({"c4_steps": steps.astype(int).tolist(), "c4_interactions": inter.tolist(),
-                  "eval_t": EVAL_T, "descent": trace})
-    return table
-
-
-def tune(mode: str = "fp64", total_particles: int = 1 << 20, reps: int = 3, verbose: bool = True) -> dict:
-    """FP64 probe tuning: per N bucket a homogeneous ensemble of about
-    total_particles particles; per active bucket every candidate timed with
-    the bucket's C4 active count forced on every system (best of reps)."""
-    steps, inter = record_mixture(mode, t_end=RECORD_T[mode], verbose=verbose)
-    ig_tab = np.zeros((NB_N, NB_A), dtype=int)
-    ch_tab = np.zeros((NB_N, NB_A), dtype=int)
-    jt_tab = np.full((NB_N, NB_A), 256, dtype=int)
-    rate_tab = np.zeros((NB_N, NB_A))
-    nact_tab = np.zeros((NB_N, NB_A), dtype=int)
-    for b, n in enumerate(N_REP):
-        E, k = probe_ensemble(mode, n, total_particles)
-        with E:
-            for a in range(NB_A):
-                if steps[b, a] > 0:   # interaction-weighted mean active count of the bucket
-                    nact = int(round(inter[b, a] / steps[b, a] / n))
-                    nact = max(A_LO[a], min(nact, (A_LO[a + 1] - 1) if a + 1 < NB_A else nact))
-                else:
-                    nact = A_REP[a]
-                nact = max(1, min(nact, n))
-                nact_tab[b, a] = nact
-                cands = candidates(mode, n, nact)
-                times = [time_candidate(E, nact, c, reps) for c in cands]
-                best = min(times)
-                pick = next(i for i, t in enumerate(times) if t <= best * (1.0 + PROBE_TIE))
-                ig, chunk, jt = cands[pick]
-                ig_tab[b, a], ch_tab[b, a], jt_tab[b, a] = ig, chunk, jt
-                rate_tab[b, a] = k * nact * n / (times[pick] * 1e-3)
-                if verbose:
-                    print(f"{mode} N={n:6d} nact={nact:6d} systems={k:4d} weight={inter[b, a]:.2e}: ig={ig} "
-                          f"chunk={chunk:6d} jtile={jt} {times[pick]:8.4f} ms (best {best:8.4f}) "
-                          f"{rate_tab[b, a]:.3e} int/s", flush=True)
-    table = {"ig": ig_tab.tolist(), "chunk": ch_tab.tolist(), "jtile": jt_tab.tolist(),
-             "interactions_per_s": rate_tab.tolist(), "n_rep": N_REP, "nact_probe": nact_tab.tolist(),
-             "c4_steps": steps.astype(int).tolist(), "c4_interactions": inter.tolist()}
+                  "eval_t": t_eval, "descent": trace})
     return table
 
 
@@ -239,10 +183,16 @@ def main():
     t0 = time.time()
     out = {"generated_by": "python -m gravidy_gb300.autotune", "modes": {}}
     for mode in args.modes.split(","):
-        out["modes"][mode] = tune_mixed() if mode == "mixed" else tune(mode)
+        table = tune_descent(mode)
         if not args.no_validate:
-            out["modes"][mode]["c4_validation"] = validate_c4(mode, out["modes"][mode], VALIDATE_T[mode])
-            print(mode, "C4 validation:", out["modes"][mode]["c4_validation"], flush=True)
+            val = validate_c4(mode, table, VALIDATE_T[mode])
+            table["c4_validation"] = val
+            print(mode, "C4 validation:", val, flush=True)
+            if val["tuned"]["device_seconds"] > val["default"]["device_seconds"] * (1.0 - TIE):
+                table.update({k: v for k, v in default_table(mode).items()})
+                table["kept"] = "default"
+                print(mode, "tuned table not faster than the default: default kept", flush=True)
+        out["modes"][mode] = table
     out["seconds"] = time.time() - t0
     with open(args.out, "w") as fh:
         json.dump(out, fh, indent=1)

@@ -102,6 +102,7 @@ struct Dev {
     double *f, *old, *a2, *a3, *t, *dt;
     double *tn;                  // t + dt of every particle (exact::add), set by the corrector
     float4 *jf0, *jf1, *jf2;
+    float4 *cs;                  // [4][total] mixed form: corrected state in FP32 form (store_cs)
     float4 *jd;                  // [5][jtotal] duplicated j data of the block-tiled items, each system's
                                  // at joff, padded to npad with zero-mass far-away particles
     int jtotal;
@@ -378,11 +379,10 @@ __device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *re
 }
 
 // ---- phase B (grid-wide): predictor of one particle of a stepping system ----
-// The mixed form's predictor: the same Taylor polynomials in FP64, evaluated
-// with fused multiply-adds and 1/6 as a multiplication (about half the FP64
-// instructions of the reference-order form, which the FP64 and exact forms
-// keep for parity); the ensemble predicts every particle of every stepping
-// system each iteration, so this phase is FP64-pipe bound.
+// The mixed form's corrector predictor: the same Taylor polynomials in FP64,
+// evaluated with fused multiply-adds and 1/6 as a multiplication (about half
+// the FP64 instructions of the reference-order form, which the FP64 and exact
+// forms keep for parity).
 __device__ __forceinline__ void predict_fma(double itime, double t, const double *f, const dbl4 &r, const dbl4 &v,
                                             dbl4 &pr, dbl4 &pv) {
     const double dt = itime - t;
@@ -398,28 +398,89 @@ __device__ __forceinline__ void predict_fma(double itime, double t, const double
     pv.w = 0.0;
 }
 
+// Mixed form: the corrected state of particle g in FP32 form, written by the
+// corrector for its particles only -- position as a double-single hi/lo pair
+// (exact::ds_split), mass, and velocity, acceleration and jerk rounded to
+// FP32, in four planes of the cs array:
+//   (x_hi, y_hi, z_hi, m) (x_lo, y_lo, z_lo, vx) (vy, vz, ax, ay) (az, jx, jy, jz)
+__device__ __forceinline__ void store_cs(const Dev &d, size_t g, const dbl4 &r, const dbl4 &v, const double f[6]) {
+    const size_t tp = (size_t)d.total;
+    float4 c0, c1;
+    exact::ds_split(r.x, c0.x, c1.x);
+    exact::ds_split(r.y, c0.y, c1.y);
+    exact::ds_split(r.z, c0.z, c1.z);
+    c0.w = (float)r.w;
+    c1.w = (float)v.x;
+    d.cs[g] = c0;
+    d.cs[tp + g] = c1;
+    d.cs[2 * tp + g] = make_float4((float)v.y, (float)v.z, (float)f[0], (float)f[1]);
+    d.cs[3 * tp + g] = make_float4((float)f[2], (float)f[3], (float)f[4], (float)f[5]);
+}
+
+// hi + lo + x as a renormalised double-single pair: Knuth's two-sum of hi and
+// x, the low parts added, then a fast two-sum (|s| >= |l|).
+__device__ __forceinline__ void ds_add(float hi, float lo, float x, float &ohi, float &olo) {
+    const float s = __fadd_rn(hi, x);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    const float l = __fadd_rn(lo, e);
+    ohi = __fadd_rn(s, l);
+    olo = __fsub_rn(l, __fsub_rn(ohi, s));
+}
+
+// Mixed form: the j data of particle g at the block time from its FP32-form
+// state -- the Taylor terms of the displacement and the velocity in FP32 (the
+// step dt = itime - t formed in FP64), the displacement added to the
+// double-single position.  The terms carry FP32 rounding relative to the
+// displacement since the particle's last step, far below the FP32 error of
+// a pair's force, so the predictor needs no FP64 arithmetic: every particle
+// of every stepping system goes through it each iteration.
+__device__ __forceinline__ void predict_ds(const Dev &d, const System &S, size_t g, float4 &a, float4 &b,
+                                           float4 &c) {
+    const size_t tp = (size_t)d.total;
+    const float4 c0 = d.cs[g], c1 = d.cs[tp + g], c2 = d.cs[2 * tp + g], c3 = d.cs[3 * tp + g];
+    const float dt = __double2float_rn(exact::sub(S.itime, d.t[g]));
+    const float dt2 = 0.5f * dt * dt;
+    const float dt3 = dt2 * dt * (1.0f / 3.0f);
+    ds_add(c0.x, c1.x, fmaf(dt3, c3.y, fmaf(dt2, c2.z, dt * c1.w)), a.x, b.x);
+    ds_add(c0.y, c1.y, fmaf(dt3, c3.z, fmaf(dt2, c2.w, dt * c2.x)), a.y, b.y);
+    ds_add(c0.z, c1.z, fmaf(dt3, c3.w, fmaf(dt2, c3.x, dt * c2.y)), a.z, b.z);
+    a.w = c0.w;
+    b.w = 0.f;
+    c = make_float4(fmaf(dt2, c3.y, fmaf(dt, c2.z, c1.w)), fmaf(dt2, c3.z, fmaf(dt, c2.w, c2.x)),
+                    fmaf(dt2, c3.w, fmaf(dt, c3.x, c2.y)), 0.f);
+}
+
 template <int MODE>
 __device__ __forceinline__ void predict_one(const Dev &d, const System &S, size_t g, bool from_state) {
-    dbl4 pr, pv;
-    if (from_state) {   // Hermite4::init_data predictors (Hermite4.cpp:202-214)
-        pr = d.r[g];
-        pr.w = (double)(float)pr.w;
-        pv = d.v[g];
-        pv.w = 0.0;
-    } else if (MODE == H4_FORCE_MIXED) {
-        predict_fma(S.itime, d.t[g], d.f + 6 * g, d.r[g], d.v[g], pr, pv);
-    } else {
-        exact::predict(S.itime, d.t[g], d.f + 6 * g, d.r[g], d.v[g], pr, pv);
-    }
-    if (MODE != H4_FORCE_MIXED) {   // the mixed corrector recomputes its particles' predictors
+    if (MODE != H4_FORCE_MIXED) {
+        dbl4 pr, pv;
+        if (from_state) {   // Hermite4::init_data predictors (Hermite4.cpp:202-214)
+            pr = d.r[g];
+            pr.w = (double)(float)pr.w;
+            pv = d.v[g];
+            pv.w = 0.0;
+        } else {
+            exact::predict(S.itime, d.t[g], d.f + 6 * g, d.r[g], d.v[g], pr, pv);
+        }
         d.pr[g] = pr;
         d.pv[g] = pv;
-    } else {
-        float4 a, b, cc;
+        return;
+    }
+    float4 a, b, cc;
+    if (from_state) {
+        dbl4 pr = d.r[g], pv = d.v[g];
+        pr.w = (double)(float)pr.w;
         exact::pack_jf(pr, pv, a, b, cc);
-        d.jf0[g] = a;
-        d.jf1[g] = b;
-        d.jf2[g] = cc;
+    } else {
+        predict_ds(d, S, g, a, b, cc);
+    }
+    // jf0-jf2 (the warp items' j, every force item's i particles), and the
+    // duplicated planes only when this step's force work is block-tiled items
+    d.jf0[g] = a;
+    d.jf1[g] = b;
+    d.jf2[g] = cc;
+    if (S.bitems) {
         const size_t tp = (size_t)d.jtotal, gj = (size_t)S.joff + (g - (size_t)S.off);
         d.jd[gj] = make_float4(a.x, a.x, a.y, a.y);
         d.jd[tp + gj] = make_float4(a.z, a.z, a.w, a.w);
@@ -500,12 +561,12 @@ __device__ bool block_item(const Dev &d, const System &S, unsigned local, float4
     const float4 *jf0 = d.jf0 + S.off, *jf1 = d.jf1 + S.off, *jf2 = d.jf2 + S.off;
     const IPair ip = pack_pair(load_i(jf0, jf1, jf2, move[min(k0, nact - 1)]),
                                load_i(jf0, jf1, jf2, move[min(k1, nact - 1)]));
+    const size_t jtp = (size_t)d.jtotal;
     const float e2f = (float)S.e2;
     const f2 e2 = pk2(e2f, e2f), m3 = pk2(-3.0f, -3.0f);
     f2 Sum[6], Cmp[6];
 #pragma unroll
     for (int c = 0; c < 6; c++) { Sum[c] = 0ull; Cmp[c] = 0ull; }
-    const size_t jtp = (size_t)d.jtotal;
     const float4 *src = d.jd + (size_t)S.joff + jb;
     const unsigned g0 = gt;   // the item's first tile
     bool ok = true;
@@ -744,6 +805,7 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
         d.dt[g] = dt0;
         d.t[g] = 0.0;
         d.tn[g] = exact::add(0.0, dt0);
+        if (MODE == H4_FORCE_MIXED) store_cs(d, g, d.r[g], d.v[g], fn);
         return;
     }
     double o[6];
@@ -768,6 +830,7 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
     d.t[g] = S.itime;
     d.dt[g] = ndt;
     d.tn[g] = exact::add(S.itime, ndt);
+    if (MODE == H4_FORCE_MIXED) store_cs(d, g, r, v, fn);
     if (!ok) {
         atomicOr(&S.err, (unsigned)H4_ERRBIT_NONFINITE);
         atomicOr(d.err, (unsigned)H4_ERRBIT_NONFINITE);
@@ -1309,7 +1372,9 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     EA(d.bucket, 2 * NB_N * NB_A); EA(d.forced_nact, 1); EA(d.launches, 1);
     EA(d.phase_ns, 4);
     EA(d.epot_i, total); EA(d.energy, 2 * nsys);
-    if (mode == H4_FORCE_MIXED) { EA(d.jf0, total); EA(d.jf1, total); EA(d.jf2, total); EA(d.jd, 5 * joff); }
+    if (mode == H4_FORCE_MIXED) {
+        EA(d.jf0, total); EA(d.jf1, total); EA(d.jf2, total); EA(d.jd, 5 * joff); EA(d.cs, 4 * total);
+    }
 #undef EA
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->own, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&E->e0);

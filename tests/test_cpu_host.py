@@ -147,21 +147,24 @@ def test_committed_tuning_table_is_well_formed():
 
 
 def test_autotuner_candidates_are_valid_table_entries():
-    """Every candidate the tuner may write passes the same rules as the
-    committed table (the library's tuning_valid), and both tuners exist."""
+    """Every candidate the descent may write passes the same rules as the
+    committed table (the library's tuning_valid), for both forms."""
     from gravidy_gb300 import autotune
-    assert callable(autotune.tune) and callable(autotune.tune_mixed)
-    for n in autotune.N_REP:
-        for a in range(len(autotune.A_LO)):
-            for ig, chunk, jt in autotune.candidates("fp64", n, autotune.A_REP[a]):
-                assert ig in (1, 2, 4) and chunk % 32 == 0 and chunk <= 2 * n
-            for ig, chunk, jt in autotune.mixed_candidates(n, a):
-                assert ig in (1, 2, 16, 32, 64, 128, 256, 512) and jt in (128, 256)
-                assert chunk % 32 == 0 and chunk <= 2 * n
-                if ig >= 16:
-                    assert chunk % jt == 0
-    d = autotune.default_table("mixed")
-    assert np.array(d["ig"]).shape == (len(autotune.N_REP), len(autotune.A_LO))
+    for mode in ("fp64", "mixed"):
+        d = autotune.default_table(mode)
+        assert np.array(d["ig"]).shape == (len(autotune.N_REP), len(autotune.A_LO))
+        for b, n in enumerate(autotune.N_REP):
+            for a in range(len(autotune.A_LO)):
+                if mode == "fp64":
+                    cands = autotune.fp64_candidates(n, a, d["chunk"][b][a])
+                    assert cands and all(ig in (2, 4) for ig, _, _ in cands)
+                else:
+                    cands = autotune.mixed_candidates(n, a)
+                for ig, chunk, jt in cands:
+                    assert ig in (1, 2, 4, 16, 32, 64, 128, 256, 512) and jt in (128, 256)
+                    assert chunk % 32 == 0 and chunk <= 2 * n
+                    if ig >= 16:
+                        assert mode == "mixed" and chunk % jt == 0
 
 
 def test_c4_sizes_are_seeded_and_in_range():

@@ -4,7 +4,9 @@
     oracle's (the reference CPU path restated) after the same block steps;
   * FP64 mode: same block-step counts and times as the single-system GPU
     path, states within 1e-9 (FP64 forces differ only in summation order);
-  * mixed mode: |dE/E| of every system within 2x of its FP64 value (+1e-9).
+  * mixed mode: |dE/E| of every system within 2x of its FP64 value (+1e-9),
+    and its state within 1e-6 of the FP64 ensemble's after a short run (the
+    mixed predictor works from an FP32 form of the corrected state).
 """
 import numpy as np
 import pytest
@@ -94,6 +96,27 @@ def test_ensemble_mixed_energy_error_close_to_fp64():
         res[mode] = np.abs((e1 - e0) / e0)
     print("dE/E fp64", res["fp64"], "mixed", res["mixed"])
     assert np.all(res["mixed"] <= 2 * res["fp64"] + 1e-9)
+
+
+def test_ensemble_mixed_state_tracks_fp64():
+    """Systems stepping with warp items (N <= 2000) and with block-tiled
+    items (N = 6000, steps of 1024 and more active) to t = 1/16: positions
+    and velocities of the mixed ensemble within 1e-6 of the FP64 ensemble's,
+    relative to the system's largest |r| and |v|."""
+    systems = _systems([700, 2000, 6000], seed0=1700)
+    st = {}
+    for mode in ("fp64", "mixed"):
+        with Ensemble(systems, mode=mode) as E:
+            E.init()
+            E.advance(0.0625)
+            st[mode] = E.download()
+            sl = [E.system_slice(c) for c in range(len(systems))]
+    for c in range(len(systems)):
+        for k in ("r", "v"):
+            a, b = st["fp64"][k][sl[c]][:, :3], st["mixed"][k][sl[c]][:, :3]
+            err = np.abs(a - b).max() / np.abs(a).max()
+            print(f"system {c} {k}: max deviation {err:.2e}")
+            assert err < 1e-6, (c, k, err)
 
 
 def test_ensemble_tune_probe_leaves_state_unchanged():
