@@ -792,6 +792,77 @@ __device__ __forceinline__ bool correct_ok(const Dev &d, const System &S, unsign
     return in_range(d, BS_MOVE, i, i + 1ll, S.n);
 }
 
+// Mixed form's corrector: the quantities of Hermite4CPU::correction_pos_vel
+// (Hermite4CPU.cpp:370-411), NbodyUtils::get_timestep_normal
+// (NbodyUtils.cpp:337-365) and NbodyUtils::normalize_dt (NbodyUtils.cpp:371-
+// 424) as exact::correct forms them, evaluated with fused multiply-adds and
+// reciprocal powers of dt, and the timestep test on the square of the
+// criterion, q = eta (|a| |a2| + |j|^2) / (|j| |a3| + |a2|^2), against the
+// squares of the candidate steps: two FP64 square roots and one division
+// where the reference order takes five and one.  A NaN q fails every test,
+// as a NaN step does in the reference (the old step is kept).
+__device__ __forceinline__ double normalize_dt_sq(double q, double old_dt, double t, double dt_min, double dt_max) {
+    const double s1 = old_dt * old_dt;   // squares of old_dt / 8, / 4, / 2, x 1, x 2
+    const double s8 = s1 * 0.015625, s4 = s1 * 0.0625, s2 = s1 * 0.25, s2x = s1 * 4.0;
+    double nd;
+    if (q <= s8) {
+        nd = exact::D_TIME_MIN_REF;
+    } else if (s8 < q && q <= s4) {
+        nd = old_dt * 0.125;
+    } else if (s4 < q && q <= s2) {
+        nd = old_dt * 0.25;
+    } else if (s2 < q && q <= s1) {
+        nd = old_dt * 0.5;
+    } else if (s1 < q && q <= s2x) {
+        nd = old_dt;
+    } else if (s2x < q) {
+        const double o2x = old_dt * 2.0;
+        const double val = exact::is_pow2(o2x) ? t * exact::recip_pow2(o2x) : t / o2x;
+        nd = (ceil(val) == val) ? o2x : old_dt;
+    } else {
+        nd = old_dt;
+    }
+    return nd < dt_min ? dt_min : (nd > dt_max ? dt_max : nd);
+}
+
+__device__ __forceinline__ bool correct_mixed(double itime, double eta, double dt_min, double dt_max, const double f[6],
+                                              const double o[6], const dbl4 &p, const dbl4 &pv, double dt1, dbl4 &r,
+                                              dbl4 &v, double a2[3], double a3[3], double &new_dt) {
+    const double dt2 = dt1 * dt1, dt3 = dt2 * dt1, dt4 = dt2 * dt2, dt5 = dt4 * dt1;
+    double i2, i3;
+    if (exact::is_pow2(dt1) && exact::is_pow2(dt5)) {   // block steps: exact reciprocals
+        i2 = exact::recip_pow2(dt2);
+        i3 = exact::recip_pow2(dt3);
+    } else {
+        const double i1 = 1.0 / dt1;
+        i2 = i1 * i1;
+        i3 = i2 * i1;
+    }
+    const double dt6 = 6.0 * dt1;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const double da = o[c] - f[c];
+        a2[c] = fma(-6.0, da, -dt1 * fma(4.0, o[3 + c], 2.0 * f[3 + c])) * i2;
+        a3[c] = fma(12.0, da, dt6 * (o[3 + c] + f[3 + c])) * i3;
+    }
+    const double c24 = dt4 * (1.0 / 24.0), c120 = dt5 * (1.0 / 120.0), c6 = dt3 * (1.0 / 6.0);
+    r.x = fma(c120, a3[0], fma(c24, a2[0], p.x));
+    r.y = fma(c120, a3[1], fma(c24, a2[1], p.y));
+    r.z = fma(c120, a3[2], fma(c24, a2[2], p.z));
+    v.x = fma(c24, a3[0], fma(c6, a2[0], pv.x));
+    v.y = fma(c24, a3[1], fma(c6, a2[1], pv.y));
+    v.z = fma(c24, a3[2], fma(c6, a2[2], pv.z));
+    // the criterion at the end of the step: a2 + dt a3
+    const double bx = fma(dt1, a3[0], a2[0]), by = fma(dt1, a3[1], a2[1]), bz = fma(dt1, a3[2], a2[2]);
+    const double A2 = fma(f[0], f[0], fma(f[1], f[1], f[2] * f[2]));
+    const double J2 = fma(f[3], f[3], fma(f[4], f[4], f[5] * f[5]));
+    const double B2 = fma(bx, bx, fma(by, by, bz * bz));
+    const double C2 = fma(a3[0], a3[0], fma(a3[1], a3[1], a3[2] * a3[2]));
+    const double q = eta * (sqrt(A2 * B2) + J2) / (sqrt(J2 * C2) + B2);
+    new_dt = normalize_dt_sq(q, dt1, itime, dt_min, dt_max);
+    return isfinite(r.x) && isfinite(r.y) && isfinite(r.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
+}
+
 // fn: the sum of the particle's partial forces (exact::sum_partials_*).
 template <int MODE>
 __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k, bool init, const double fn[6]) {
@@ -821,8 +892,10 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
         pr = d.pr[g];
         pv = d.pv[g];
     }
-    const bool ok = exact::correct(S.itime, S.eta, S.dt_min, S.dt_max, fn, o, pr, pv, d.dt[g], r, v, a2,
-                                   a3, ndt);
+    const bool ok = MODE == H4_FORCE_MIXED
+                        ? correct_mixed(S.itime, S.eta, S.dt_min, S.dt_max, fn, o, pr, pv, d.dt[g], r, v, a2, a3, ndt)
+                        : exact::correct(S.itime, S.eta, S.dt_min, S.dt_max, fn, o, pr, pv, d.dt[g], r, v, a2, a3,
+                                         ndt);
     d.r[g] = r;
     d.v[g] = v;
 #pragma unroll
@@ -868,6 +941,7 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
     __shared__ unsigned red[WARPS];
     __shared__ double redd[WARPS];
     __shared__ unsigned s_item[WARPS];
+    __shared__ double s_fn[32][6];   // phase D: reduced forces of a group of warp-reduced particles
     __shared__ unsigned s_bitem;
     // barriers of the block-item stages and of the warps' rings
     __shared__ __align__(8) uint64_t s_full[NS], s_empty[NS], s_wfull[WARPS][WARP_STAGES];
@@ -973,14 +1047,33 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
         // D: corrector of every active particle; the partial forces of
         // systems with many j-chunks are summed by a warp per particle
         // (lane 0 corrects), the others by a thread per particle
-        for (unsigned a = gtid >> 5; a < c_aw; a += nthreads >> 5) {
-            const int c = find_seg(s_actw, d.nsys, a);
-            System &S = d.sys[c];
-            const unsigned k = a - s_actw[c];
-            if (!__all_sync(0xffffffffu, correct_ok(d, S, k))) continue;
-            double fn[6];
-            exact::sum_partials_warp(d.part + S.part_off, S.nact, k, S.split, lane, fn);
-            if (lane == 0) correct_one<MODE>(d, S, k, init != 0, fn);
+        // (groups of 32 particles per block: each warp reduces four into
+        // shared memory, then one warp corrects the 32 with every lane busy
+        // -- an FP64 corrector on one lane of a warp takes the FP64 pipe as
+        // long as a full warp)
+        for (unsigned grp = blockIdx.x; grp * 32u < c_aw; grp += gridDim.x) {
+            for (unsigned q = (unsigned)w; q < 32u; q += WARPS) {
+                const unsigned a = grp * 32u + q;
+                if (a >= c_aw) break;
+                const int c = find_seg(s_actw, d.nsys, a);
+                const System &S = d.sys[c];
+                const unsigned k = a - s_actw[c];
+                if (!__all_sync(0xffffffffu, correct_ok(d, S, k))) continue;
+                double fn[6];
+                exact::sum_partials_warp(d.part + S.part_off, S.nact, k, S.split, lane, fn);
+                if (lane == 0)
+#pragma unroll
+                    for (int x = 0; x < 6; x++) s_fn[q][x] = fn[x];
+            }
+            __syncthreads();
+            if (w == 0 && grp * 32u + (unsigned)lane < c_aw) {
+                const unsigned a = grp * 32u + (unsigned)lane;
+                const int c = find_seg(s_actw, d.nsys, a);
+                System &S = d.sys[c];
+                const unsigned k = a - s_actw[c];
+                if (correct_ok(d, S, k)) correct_one<MODE>(d, S, k, init != 0, s_fn[lane]);
+            }
+            __syncthreads();
         }
         for (unsigned a = gtid; a < c_at; a += nthreads) {
             const int c = find_seg(s_actt, d.nsys, a);
