@@ -102,7 +102,7 @@ struct Dev {
     int nsys, total;
     System *sys;
     dbl4 *r, *v, *pr, *pv;
-    double *f, *old, *a2, *a3, *t, *dt;
+    double *f, *t, *dt;          // forces (a, jerk), time, timestep
     double *tn;                  // t + dt of every particle (exact::add), set by the corrector
     float4 *jf0, *jf1, *jf2;
     float4 *cs;                  // [4][total] mixed form: corrected state in FP32 form (store_cs)
@@ -882,10 +882,9 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
         if (MODE == H4_FORCE_MIXED) store_cs(d, g, d.r[g], d.v[g], fn);
         return;
     }
-    double o[6];
-    double *op = d.old + 6 * g;
+    double o[6];   // the old forces (the reference's old_a/old_a1), read before they are replaced
 #pragma unroll
-    for (int q = 0; q < 6; q++) { o[q] = fp[q]; op[q] = o[q]; fp[q] = fn[q]; }
+    for (int q = 0; q < 6; q++) { o[q] = fp[q]; fp[q] = fn[q]; }
     dbl4 r = d.r[g], v = d.v[g];
     double a2[3], a3[3], ndt;
     dbl4 pr, pv;
@@ -901,8 +900,6 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
                                          ndt);
     d.r[g] = r;
     d.v[g] = v;
-#pragma unroll
-    for (int q = 0; q < 3; q++) { d.a2[3 * g + q] = a2[q]; d.a3[3 * g + q] = a3[q]; }
     d.t[g] = S.itime;
     d.dt[g] = ndt;
     d.tn[g] = exact::add(S.itime, ndt);
@@ -1460,7 +1457,7 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
     e = cudaSuccess;
 #define EA(p, cnt) if (e == cudaSuccess) e = dalloc(E, &p, cnt)
     EA(d.sys, nsys); EA(d.r, total); EA(d.v, total); EA(d.pr, total); EA(d.pv, total);
-    EA(d.f, 6 * total); EA(d.old, 6 * total); EA(d.a2, 3 * total); EA(d.a3, 3 * total);
+    EA(d.f, 6 * total);
     d.part_total = part_total;
     EA(d.t, total); EA(d.dt, total); EA(d.tn, total); EA(d.move, total); EA(d.part, part_total);
     EA(d.queue, 1); EA(d.queue_b, 1); EA(d.bar_count, 1); EA(d.bar_gen, 1); EA(d.err, 2);
@@ -1493,9 +1490,9 @@ int h4_ens_create(h4_ens_handle *out, unsigned int nsys, const unsigned int *n, 
         k_ens_pad_jd<<<std::min(nsys, 4096u), THREADS, 0, s>>>(d);
         e = cudaGetLastError();
     }
-    void *zero[] = {d.f, d.old, d.a2, d.a3, d.t, d.dt, d.tn};
-    size_t zb[] = {48 * total, 48 * total, 24 * total, 24 * total, 8 * total, 8 * total, 8 * total};
-    for (int k = 0; k < 7 && e == cudaSuccess; k++) e = cudaMemsetAsync(zero[k], 0, zb[k], s);
+    void *zero[] = {d.f, d.t, d.dt, d.tn};
+    size_t zb[] = {48 * total, 8 * total, 8 * total, 8 * total};
+    for (int k = 0; k < 4 && e == cudaSuccess; k++) e = cudaMemsetAsync(zero[k], 0, zb[k], s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.queue, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.queue_b, 0, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d.bar_count, 0, 4, s);
