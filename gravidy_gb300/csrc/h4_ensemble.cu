@@ -94,6 +94,10 @@ struct System {
     // (split = bsplit * q partials per particle)
     unsigned bitems, jt, q, bsplit;
     unsigned done, err;
+    // the next block time without a scan (bit patterns of tn): the least tn
+    // of the particles that did not step (phase A's compaction) and of those
+    // corrected since (phase D, atomic minimum)
+    unsigned long long tmin_idle, tmin_stepped;
     size_t part_off, part_cap;   // partial-force area (doubles)
     unsigned long long steps, psteps, inter;
 };
@@ -244,31 +248,25 @@ __device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *re
         for (int i = threadIdx.x; i < na; i += THREADS) d.move[off + i] = (unsigned)i;
         nact = (unsigned)na;
         itime = init ? 0.0 : S.itime;
+        if (init && threadIdx.x == 0) {   // every particle is corrected: its tn enters tmin_stepped
+            S.tmin_idle = exact::INF_BITS;
+            S.tmin_stepped = exact::INF_BITS;
+        }
     } else {
         if (S.done) {
             if (threadIdx.x == 0) { S.items = 0; S.bitems = 0; S.nact = 0; }
             return;
         }
         // Hermite4::next_integration_time (Hermite4.cpp:90-102) for this
-        // system: the least t + dt, as the least bit pattern of the stored
-        // tn (t + dt > 0; a NaN pattern sorts above +inf, as fmin ignores
-        // NaN) -- integer work, where FP64 adds and minima on one SM would
-        // take longer than the rest of the phase
+        // system: the least t + dt over its particles, as the least bit
+        // pattern of the stored tn (t + dt > 0; a NaN pattern sorts above
+        // +inf, as fmin ignores NaN): the least over the particles that did
+        // not step last time (recorded by the last compaction) and over those
+        // corrected since (atomic minimum of the corrector) -- integer work
+        // and no scan, where FP64 adds and minima on one SM would take longer
+        // than the rest of the phase
         const unsigned long long *tnb = reinterpret_cast<const unsigned long long *>(d.tn + off);
-        unsigned long long mb = exact::INF_BITS;
-#pragma unroll 4
-        for (int i = threadIdx.x; i < n; i += THREADS) mb = min(mb, tnb[i]);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mb = min(mb, __shfl_down_sync(0xffffffffu, mb, o));
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        unsigned long long *redb = reinterpret_cast<unsigned long long *>(redd);
-        __syncthreads();
-        if (lane == 0) redb[w] = mb;
-        __syncthreads();
-        mb = redb[0];
-        for (int k = 1; k < WARPS; k++) mb = min(mb, redb[k]);
-        __syncthreads();
-        const double m = exact::bits_to_double(mb);
+        const double m = exact::bits_to_double(min(S.tmin_idle, S.tmin_stepped));
         // the reference's loop condition, on the last step's block time
         const bool stop = S.err != 0u || !(S.itime < S.t_end);
         if (stop) {
@@ -280,25 +278,44 @@ __device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *re
         // |itime - tn| < 2^-51 as a window of bit patterns
         unsigned long long wlo = 0, whi = 0;
         const bool window = exact::active_window(itime, wlo, whi);
-        // ascending compaction, 8 particles per thread per round
-        for (int base = 0; base < n; base += THREADS * 8) {
-            unsigned flags = 0, cnt = 0;
-            const int i0 = base + threadIdx.x * 8;
+        // ascending compaction, 32 particles per thread per round, and the
+        // least tn of the particles that do not step
+        unsigned long long idle = exact::INF_BITS;
+        for (int base = 0; base < n; base += THREADS * 32) {
+            unsigned flags = 0;
+            const int i0 = base + threadIdx.x * 32;
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
+            for (int q = 0; q < 32; q++) {
                 const int i = i0 + q;
-                if (i < n && (window ? tnb[i] - wlo <= whi - wlo : exact::is_active_tn(itime, d.tn[off + i]))) {
-                    flags |= 1u << q;
-                    cnt++;
+                if (i < n) {
+                    const unsigned long long b = tnb[i];
+                    if (window ? b - wlo <= whi - wlo : exact::is_active_tn(itime, exact::bits_to_double(b)))
+                        flags |= 1u << q;
+                    else
+                        idle = min(idle, b);
                 }
             }
             unsigned tot;
+            const unsigned cnt = (unsigned)__popc(flags);
             unsigned pos = nact + block_scan_u(cnt, red, &tot);
             if (cnt && !in_range(d, BS_SCATTER, pos, (long long)pos + cnt, n)) flags = 0;
-#pragma unroll
-            for (int q = 0; q < 8; q++)
-                if (flags & (1u << q)) d.move[off + pos++] = (unsigned)(i0 + q);
+            while (flags) {
+                const int q = __ffs(flags) - 1;
+                flags &= flags - 1u;
+                d.move[off + pos++] = (unsigned)(i0 + q);
+            }
             nact += tot;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) idle = min(idle, __shfl_down_sync(0xffffffffu, idle, o));
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        unsigned long long *redb = reinterpret_cast<unsigned long long *>(redd);
+        if (lane == 0) redb[w] = idle;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 1; k < WARPS; k++) idle = min(idle, redb[k]);
+            S.tmin_idle = idle;
+            S.tmin_stepped = exact::INF_BITS;
         }
     }
     if (threadIdx.x == 0) {
@@ -587,7 +604,7 @@ __device__ bool block_item(const Dev &d, const System &S, unsigned local, float4
             f2 part[6];
 #pragma unroll
             for (int c = 0; c < 6; c++) part[c] = 0ull;
-#pragma unroll 4
+#pragma unroll 16   // measured: 7.7e11 pairs/s against 7.5e11 (8) and 7.1e11 (4)
             for (int u = 0; u < sub; u++) {
                 const int jj = (int)qq + (sb + u) * (int)Q;
                 const f2 *q0 = (const f2 *)&sj[b][0][jj], *q1 = (const f2 *)&sj[b][1][jj],
@@ -868,7 +885,9 @@ __device__ __forceinline__ bool correct_mixed(double itime, double eta, double d
 
 // fn: the sum of the particle's partial forces (exact::sum_partials_*).
 template <int MODE>
-__device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k, bool init, const double fn[6]) {
+// Returns the bit pattern of the particle's new tn = t + dt.
+__device__ __forceinline__ unsigned long long correct_one(const Dev &d, System &S, unsigned k, bool init,
+                                                          const double fn[6]) {
     const unsigned i = d.move[S.off + k];
     const size_t g = (size_t)S.off + i;
     double *fp = d.f + 6 * g;
@@ -878,9 +897,10 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
         const double dt0 = exact::init_dt(fn, (double)0.01f, S.dt_min, S.dt_max);
         d.dt[g] = dt0;
         d.t[g] = 0.0;
-        d.tn[g] = exact::add(0.0, dt0);
+        const double tn0 = exact::add(0.0, dt0);
+        d.tn[g] = tn0;
         if (MODE == H4_FORCE_MIXED) store_cs(d, g, d.r[g], d.v[g], fn);
-        return;
+        return exact::double_to_bits(tn0);
     }
     double o[6];   // the old forces (the reference's old_a/old_a1), read before they are replaced
 #pragma unroll
@@ -902,11 +922,28 @@ __device__ __forceinline__ void correct_one(const Dev &d, System &S, unsigned k,
     d.v[g] = v;
     d.t[g] = S.itime;
     d.dt[g] = ndt;
-    d.tn[g] = exact::add(S.itime, ndt);
+    const double tn = exact::add(S.itime, ndt);
+    d.tn[g] = tn;
     if (MODE == H4_FORCE_MIXED) store_cs(d, g, r, v, fn);
     if (!ok) {
         atomicOr(&S.err, (unsigned)H4_ERRBIT_NONFINITE);
         atomicOr(d.err, (unsigned)H4_ERRBIT_NONFINITE);
+    }
+    return exact::double_to_bits(tn);
+}
+
+// The corrected particles' tn into their systems' tmin_stepped: one atomic
+// per warp when its lanes share a system (c < 0: lane without a particle).
+// Called by every lane of the warp.
+__device__ __forceinline__ void fold_tmin(const Dev &d, int c, unsigned long long tnb) {
+    const int c0 = __shfl_sync(0xffffffffu, c, 0);
+    if (__all_sync(0xffffffffu, c == c0 || c < 0)) {
+        unsigned long long m = c < 0 ? exact::INF_BITS : tnb;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_down_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0 && c0 >= 0) atomicMin(&d.sys[c0].tmin_stepped, m);
+    } else if (c >= 0) {
+        atomicMin(&d.sys[c].tmin_stepped, tnb);
     }
 }
 
@@ -1066,23 +1103,40 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
                     for (int x = 0; x < 6; x++) s_fn[q][x] = fn[x];
             }
             __syncthreads();
-            if (w == 0 && grp * 32u + (unsigned)lane < c_aw) {
+            if (w == 0) {
                 const unsigned a = grp * 32u + (unsigned)lane;
-                const int c = find_seg(s_actw, d.nsys, a);
-                System &S = d.sys[c];
-                const unsigned k = a - s_actw[c];
-                if (correct_ok(d, S, k)) correct_one<MODE>(d, S, k, init != 0, s_fn[lane]);
+                int cs = -1;
+                unsigned long long tnb = exact::INF_BITS;
+                if (a < c_aw) {
+                    const int c = find_seg(s_actw, d.nsys, a);
+                    System &S = d.sys[c];
+                    const unsigned k = a - s_actw[c];
+                    if (correct_ok(d, S, k)) {
+                        tnb = correct_one<MODE>(d, S, k, init != 0, s_fn[lane]);
+                        cs = c;
+                    }
+                }
+                fold_tmin(d, cs, tnb);
             }
             __syncthreads();
         }
-        for (unsigned a = gtid; a < c_at; a += nthreads) {
-            const int c = find_seg(s_actt, d.nsys, a);
-            System &S = d.sys[c];
-            const unsigned k = a - s_actt[c];
-            if (!correct_ok(d, S, k)) continue;
-            double fn[6];
-            exact::sum_partials_thread(d.part + S.part_off, S.nact, k, S.split, fn);
-            correct_one<MODE>(d, S, k, init != 0, fn);
+        // (warp-uniform trip count, for fold_tmin)
+        for (unsigned a0 = gtid - (unsigned)lane; a0 < c_at; a0 += nthreads) {
+            const unsigned a = a0 + (unsigned)lane;
+            int cs = -1;
+            unsigned long long tnb = exact::INF_BITS;
+            if (a < c_at) {
+                const int c = find_seg(s_actt, d.nsys, a);
+                System &S = d.sys[c];
+                const unsigned k = a - s_actt[c];
+                if (correct_ok(d, S, k)) {
+                    double fn[6];
+                    exact::sum_partials_thread(d.part + S.part_off, S.nact, k, S.split, fn);
+                    tnb = correct_one<MODE>(d, S, k, init != 0, fn);
+                    cs = c;
+                }
+            }
+            fold_tmin(d, cs, tnb);
         }
         if (!grid_sync(d)) return;
         phase_mark(d, 3, t_prev);
