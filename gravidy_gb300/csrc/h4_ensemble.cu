@@ -465,11 +465,8 @@ __device__ __forceinline__ void ds_add(float hi, float lo, float x, float &ohi, 
 // displacement since the particle's last step, far below the FP32 error of
 // a pair's force, so the predictor needs no FP64 arithmetic: every particle
 // of every stepping system goes through it each iteration.
-__device__ __forceinline__ void predict_ds(const Dev &d, const System &S, size_t g, float4 &a, float4 &b,
-                                           float4 &c) {
-    const size_t tp = (size_t)d.total;
-    const float4 c0 = d.cs[g], c1 = d.cs[tp + g], c2 = d.cs[2 * tp + g], c3 = d.cs[3 * tp + g];
-    const float dt = __double2float_rn(exact::sub(S.itime, d.t[g]));
+__device__ __forceinline__ void predict_ds(const float4 &c0, const float4 &c1, const float4 &c2, const float4 &c3,
+                                           float dt, float4 &a, float4 &b, float4 &c) {
     const float dt2 = 0.5f * dt * dt;
     const float dt3 = dt2 * dt * (1.0f / 3.0f);
     ds_add(c0.x, c1.x, fmaf(dt3, c3.y, fmaf(dt2, c2.z, dt * c1.w)), a.x, b.x);
@@ -479,6 +476,39 @@ __device__ __forceinline__ void predict_ds(const Dev &d, const System &S, size_t
     b.w = 0.f;
     c = make_float4(fmaf(dt2, c3.y, fmaf(dt, c2.z, c1.w)), fmaf(dt2, c3.z, fmaf(dt, c2.w, c2.x)),
                     fmaf(dt2, c3.w, fmaf(dt, c3.x, c2.y)), 0.f);
+}
+
+// Last c with pre[c] <= x, over pre[0..m] (pre[0] = 0, nondecreasing).
+__device__ __forceinline__ int find_seg(const unsigned *pre, int m, unsigned x) {
+    int lo = 0, hi = m;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (pre[mid] <= x) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Writes particle g's j data (a, b, c: the jf0-jf2 records) in the layouts
+// this step's force items of its system read.
+__device__ __forceinline__ void store_jdata(const Dev &d, const System &S, size_t g, const float4 &a, const float4 &b,
+                                            const float4 &cc) {
+    // jf0-jf2 (the warp items' j, every force item's i particles), and the
+    // duplicated planes only when this step's force work is block-tiled items
+    d.jf0[g] = a;
+    d.jf1[g] = b;
+    d.jf2[g] = cc;
+    if (S.bitems) {
+        const size_t tp = (size_t)d.jtotal, gj = (size_t)S.joff + (g - (size_t)S.off);
+        d.jd[gj] = make_float4(a.x, a.x, a.y, a.y);
+        d.jd[tp + gj] = make_float4(a.z, a.z, a.w, a.w);
+        d.jd[2 * tp + gj] = make_float4(b.x, b.x, b.y, b.y);
+        d.jd[3 * tp + gj] = make_float4(b.z, b.z, cc.x, cc.x);
+        d.jd[4 * tp + gj] = make_float4(cc.y, cc.y, cc.z, cc.z);
+    }
+}
+
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
 template <int MODE>
@@ -498,37 +528,18 @@ __device__ __forceinline__ void predict_one(const Dev &d, const System &S, size_
         return;
     }
     float4 a, b, cc;
-    if (from_state) {
+    if (from_state) {   // the initial forces or a tuning probe
         dbl4 pr = d.r[g], pv = d.v[g];
         pr.w = (double)(float)pr.w;
         exact::pack_jf(pr, pv, a, b, cc);
     } else {
-        predict_ds(d, S, g, a, b, cc);
+        const size_t tp = (size_t)d.total;
+        predict_ds(d.cs[g], d.cs[tp + g], d.cs[2 * tp + g], d.cs[3 * tp + g],
+                   __double2float_rn(exact::sub(S.itime, d.t[g])), a, b, cc);
     }
-    // jf0-jf2 (the warp items' j, every force item's i particles), and the
-    // duplicated planes only when this step's force work is block-tiled items
-    d.jf0[g] = a;
-    d.jf1[g] = b;
-    d.jf2[g] = cc;
-    if (S.bitems) {
-        const size_t tp = (size_t)d.jtotal, gj = (size_t)S.joff + (g - (size_t)S.off);
-        d.jd[gj] = make_float4(a.x, a.x, a.y, a.y);
-        d.jd[tp + gj] = make_float4(a.z, a.z, a.w, a.w);
-        d.jd[2 * tp + gj] = make_float4(b.x, b.x, b.y, b.y);
-        d.jd[3 * tp + gj] = make_float4(b.z, b.z, cc.x, cc.x);
-        d.jd[4 * tp + gj] = make_float4(cc.y, cc.y, cc.z, cc.z);
-    }
+    store_jdata(d, S, g, a, b, cc);
 }
 
-// Last c with pre[c] <= x, over pre[0..m] (pre[0] = 0, nondecreasing).
-__device__ __forceinline__ int find_seg(const unsigned *pre, int m, unsigned x) {
-    int lo = 0, hi = m;
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (pre[mid] <= x) lo = mid; else hi = mid;
-    }
-    return lo;
-}
 
 // ---- P1 (mixed form): one block-tiled item --------------------------------------
 // S.ig active particles (P = S.ig / 2 packed pairs, one per thread of each of
@@ -828,9 +839,11 @@ __device__ __forceinline__ bool correct_ok(const Dev &d, const System &S, unsign
 // 424) as exact::correct forms them, evaluated with fused multiply-adds and
 // reciprocal powers of dt, and the timestep test on the square of the
 // criterion, q = eta (|a| |a2| + |j|^2) / (|j| |a3| + |a2|^2), against the
-// squares of the candidate steps: two FP64 square roots and one division
-// where the reference order takes five and one.  A NaN q fails every test,
-// as a NaN step does in the reference (the old step is kept).
+// squares of the candidate steps: q in FP32 where its inputs allow (the
+// quantised step then differs from an FP64 q only within FP32 rounding of a
+// power-of-two boundary), else two FP64 square roots and one division, where
+// the reference order takes five and one.  A NaN q fails every test, as a NaN
+// step does in the reference (the old step is kept).
 __device__ __forceinline__ double normalize_dt_sq(double q, double old_dt, double t, double dt_min, double dt_max) {
     const double s1 = old_dt * old_dt;   // squares of old_dt / 8, / 4, / 2, x 1, x 2
     const double s8 = s1 * 0.015625, s4 = s1 * 0.0625, s2 = s1 * 0.25, s2x = s1 * 4.0;
@@ -888,7 +901,20 @@ __device__ __forceinline__ bool correct_mixed(double itime, double eta, double d
     const double J2 = fma(f[3], f[3], fma(f[4], f[4], f[5] * f[5]));
     const double B2 = fma(bx, bx, fma(by, by, bz * bz));
     const double C2 = fma(a3[0], a3[0], fma(a3[1], a3[1], a3[2] * a3[2]));
-    const double q = eta * (sqrt(A2 * B2) + J2) / (sqrt(J2 * C2) + B2);
+    // the criterion in FP32 where the four squares and their products lie
+    // well inside its range (exponents within 2^+-60, tested on the bits),
+    // else in FP64
+    const auto in_f32 = [](double x) {
+        const unsigned e = (unsigned)(exact::double_to_bits(x) >> 52);   // sign 0: x >= 0
+        return e >= 1023u - 60u && e <= 1023u + 60u;
+    };
+    double q;
+    if (in_f32(A2) && in_f32(J2) && in_f32(B2) && in_f32(C2)) {
+        const float a = (float)A2, j = (float)J2, b = (float)B2, c = (float)C2;
+        q = (double)((float)eta * (sqrtf(a * b) + j) / (sqrtf(j * c) + b));
+    } else {
+        q = eta * (sqrt(A2 * B2) + J2) / (sqrt(J2 * C2) + B2);
+    }
     new_dt = normalize_dt_sq(q, dt1, itime, dt_min, dt_max);
     return isfinite(r.x) && isfinite(r.y) && isfinite(r.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
 }
@@ -1051,8 +1077,18 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
             s_actw[d.nsys] = c_aw; s_actt[d.nsys] = c_at;
         }
         __syncthreads();
-        // B: predictor of every particle of the systems taking a step
+        // B: predictor of every particle of the systems taking a step (the
+        // mixed form's inputs of a thread's next particle prefetched into L2
+        // meanwhile: its chain of loads would otherwise wait out the latency)
         for (unsigned g = gtid; g < (unsigned)d.total; g += nthreads) {
+            if (MODE == H4_FORCE_MIXED && !from_state && g + nthreads < (unsigned)d.total) {
+                const size_t gn = (size_t)g + nthreads, tp = (size_t)d.total;
+                prefetch_l2(d.cs + gn);
+                prefetch_l2(d.cs + tp + gn);
+                prefetch_l2(d.cs + 2 * tp + gn);
+                prefetch_l2(d.cs + 3 * tp + gn);
+                prefetch_l2(d.t + gn);
+            }
             const int c = find_seg(s_off, d.nsys, g);
             const System &S = d.sys[c];
             if (S.nact == 0u) continue;
