@@ -178,6 +178,15 @@ __device__ bool grid_sync(const Dev &d) {
     return (*(volatile unsigned *)d.err & H4_ERRBIT_TIMEOUT) == 0u;
 }
 
+// Partials of a particle summed by a warp (the fixed order of
+// exact::sum_partials_warp) from this many j-chunks on, by its thread (chunk
+// order) below: higher than the single-system path's threshold, so that the
+// 32-63-chunk splits of mid-sized warp-item steps stay on the thread path
+// (measured: the corrector phase of C4 355 against 491 ms, with the groups
+// of the warp path moved to the last blocks).
+constexpr unsigned ENS_WARP_REDUCE_MIN_S = 64;
+__device__ __forceinline__ bool warp_reduce(unsigned S) { return S >= ENS_WARP_REDUCE_MIN_S; }
+
 __device__ __forceinline__ int n_bucket(int n) {
     int b = 0;
     for (int lim = 512; b < NB_N - 1 && n > lim; lim <<= 1) b++;
@@ -1056,7 +1065,7 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
             const unsigned x_w = v ? d.sys[c].items : 0u;
             const unsigned x_b = v ? d.sys[c].bitems : 0u;
             const unsigned x_a = v ? d.sys[c].nact : 0u;
-            const unsigned x_aw = (v && exact::warp_reduce(d.sys[c].split)) ? x_a : 0u;
+            const unsigned x_aw = (v && warp_reduce(d.sys[c].split)) ? x_a : 0u;
             unsigned t0, t1, t2, t3, t4;
             const unsigned e0 = block_scan_u(x_off, red, &t0);
             const unsigned e1 = block_scan_u(x_w, red, &t1);
@@ -1134,7 +1143,11 @@ __global__ void __launch_bounds__(THREADS, kMinBlocks<MODE>) k_ensemble(Dev d, i
         // shared memory, then one warp corrects the 32 with every lane busy
         // -- an FP64 corrector on one lane of a warp takes the FP64 pipe as
         // long as a full warp)
-        for (unsigned grp = blockIdx.x; grp * 32u < c_aw; grp += gridDim.x) {
+        // (groups taken from the last block down: the thread path below
+        // gives particle a to thread a, so when the active particles do not
+        // fill the grid the last blocks have none, and the groups then run
+        // beside the thread path instead of after it on the same blocks)
+        for (unsigned grp = gridDim.x - 1u - blockIdx.x; grp * 32u < c_aw; grp += gridDim.x) {
             for (unsigned q = (unsigned)w; q < 32u; q += WARPS) {
                 const unsigned a = grp * 32u + q;
                 if (a >= c_aw) break;
