@@ -83,6 +83,33 @@ def test_ensemble_fp64_matches_single_system_runs():
         assert abs(etot[c] - e1) < 1e-12 * abs(e1), c
 
 
+def test_ensemble_fp64_many_chunk_steps_match_single_system_runs():
+    """A 9000-particle system beside a small one: its steps of 1-3 active
+    particles split the j range into 71 chunks of 128, so the corrector sums
+    their partials by warps, 32 particles per group on the grid's last
+    blocks.  Same steps and block times as the single-system runs, states
+    within 1e-9 (FP64 sums in another order)."""
+    systems = _systems([9000, 700], seed0=1900)
+    t_end = 0.03125
+    with Ensemble(systems, mode="fp64") as E:
+        E.init()
+        E.advance(t_end)
+        st = E.download()
+        stats = E.stats()
+        steps_b, _ = E.bucket_stats()
+    assert steps_b[5, 0] + steps_b[5, 1] > 0   # N in (8192, 16384], 1-3 active: the warp reduction ran
+    for c, (m, p, v, soft, eta) in enumerate(systems):
+        ns = NbodySystem(m, p, v, softening=soft, eta=eta)
+        with Hermite4GPU(ns) as g:
+            g.init_acc_jrk()
+            atime = g.init_dt(1.0e10, float(orc.ETA_S), 0.0)
+            itime, atime, steps, _, _, _ = g.advance(t_end, 1e30, atime)
+            s1 = g.download()
+        sl = E.system_slice(c)
+        assert int(stats["steps"][c]) == steps and stats["itime"][c] == itime, c
+        assert np.abs(st["r"][sl] - s1["r"]).max() < 1e-9, c
+
+
 def test_ensemble_mixed_energy_error_close_to_fp64():
     systems = _systems([512, 1024, 2048, 700], seed0=500)
     t_end = 0.25
