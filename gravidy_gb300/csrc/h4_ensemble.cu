@@ -3,22 +3,26 @@
 // persistent fused kernel per graph iteration.
 //
 // The per-system arithmetic is the single-system path's (exact-order
-// predictor/corrector/timestep of h4_exact.cuh, force items of h4_pair.cuh);
+// predictor/corrector/timestep of h4_exact.cuh, force items of h4_pair.cuh;
+// the mixed form's predictor and corrector in their own FP32/FMA forms below);
 // what changes is the schedule.  One iteration of k_ensemble does one block
 // step of every unfinished system, in four phases separated by grid-wide
 // barriers:
-//   A  per system (one block): next block time (min t + dt), the reference's
-//      loop condition, ordered active set, force work layout for its
-//      (N, N_act) from the tuning table: warp items (lanes over j), or in the
-//      mixed form block-tiled items (lanes over i, j tiles in shared memory);
+//   A  per system (one block): next block time (the least t + dt, kept by
+//      the corrector and the last compaction), the reference's loop
+//      condition, ordered active set (integer work on the bits of t + dt),
+//      force work layout for its (N, N_act) from the tuning table: warp items
+//      (lanes over j), or in the mixed form block-tiled items (lanes over i,
+//      j tiles in shared memory);
 //   B  all threads: predictor of every particle of the stepping systems;
 //   C  all blocks: the force sums -- block-tiled items (j tiles brought into
-//      shared memory by TMA bulk copies on an mbarrier, double buffered;
-//      packed f32x2) then warp items, each kind from one global work queue
-//      (the systems' item counts are prefix-summed in shared memory, an item
-//      finds its system by binary search);
-//   D  all threads: fixed-order reduction of the partial forces, save of the
-//      old forces, corrector and new timestep of every active particle.
+//      shared memory by TMA bulk copies, three stages on full/empty
+//      mbarriers; packed f32x2) then warp items (j through a per-warp TMA
+//      ring), each kind from one global work queue (the systems' item counts
+//      are prefix-summed in shared memory, an item finds its system by binary
+//      search);
+//   D  all threads: fixed-order reduction of the partial forces, corrector
+//      and new timestep of every active particle.
 // The O(N) and O(N_act) phases are spread over the whole GPU: FP64
 // prediction and correction of a large system on one SM would otherwise set
 // the pace of every iteration.
