@@ -3,7 +3,7 @@
 Tuned shape of a system's force work (include/gravidy_gb300.h, the tuning
 table of h4_ens_set_tuning):
   * FP64 form: particles per warp item (1, 2, 4) x j-chunk length;
-  * mixed form: warp items of 1 particle or a packed pair (lanes over j) x
+  * mixed form: warp items of 1 particle, a packed pair or two (lanes over j) x
     j-chunk length, or block-tiled items of 16 ... 512 particles (lanes over
     i, j tiles in shared memory) x j-chunk length x shared-memory j tile
     (128 or 256).
@@ -69,15 +69,16 @@ def mixed_candidates(n: int, a: int):
             for chunk in (512, 1024, 2048, 4096):
                 out.append((bti, chunk, 256))
         out += [(512, 1024, 128), (256, 1024, 128)]
-        out += [(2, 2048, 256), (2, 4096, 256)]
-    elif a >= 3:    # 16 - 255 active: packed-pair warp items or narrow blocks
+        out += [(4, 2048, 256), (4, 4096, 256), (2, 2048, 256)]
+    elif a >= 3:    # 16 - 255 active: warp items of two or one packed pairs, or narrow blocks
         for chunk in (512, 1024, 2048, 4096):
-            out.append((2, chunk, 256))
+            out.append((4, chunk, 256))
+        out += [(2, 1024, 256), (2, 2048, 256)]
         for bti in (128, 64, 32, 16):
             if bti <= 4 * A_LO[a + 1]:
                 out += [(bti, 1024, 256), (bti, 2048, 256)]
     else:           # a handful active: warp items
-        for ig in (2, 1):
+        for ig in ((4, 2, 1) if a == 2 else (2, 1)):
             for chunk in (256, 512, 1024, 2048):
                 out.append((ig, chunk, 256))
     return [c for c in out if c[1] <= 2 * n]
@@ -109,9 +110,10 @@ MIN_WEIGHT = {"mixed": 0.005, "fp64": 0.02}
 def default_table(mode: str) -> dict:
     """The library's built-in table (default_tuning in h4_ensemble.cu)."""
     ch = [128, 128, 256, 512, 1024, 2048, 4096, 8192]
-    mixed_ig = [1, 2, 2, 2, 2, 2, 512, 512]
+    mixed_ig = [1, 2, 4, 4, 4, 4, 512, 512]
+    mixed_ch = [128, 128, 1024, 1024, 1024, 1024, 1024, 1024]
     ig = [[(mixed_ig[a] if mode == "mixed" else 4) for a in range(NB_A)] for _ in range(NB_N)]
-    chunk = [[(1024 if mode == "mixed" and mixed_ig[a] > 2 else ch[a]) for a in range(NB_A)] for _ in range(NB_N)]
+    chunk = [[(mixed_ch[a] if mode == "mixed" else ch[a]) for a in range(NB_A)] for _ in range(NB_N)]
     return {"ig": ig, "chunk": chunk, "jtile": [[256] * NB_A for _ in range(NB_N)]}
 
 

@@ -387,12 +387,9 @@ __device__ void phaseA(const Dev &d, int c, bool init, unsigned *red, double *re
                 }
                 split = bsplit * q;
             } else {
-                // warp items: 1, 2 or 4 particles (FP64); 1 or 2 (mixed: a
-                // packed pair)
-                if (MODE == H4_FORCE_MIXED)
-                    ig = ig == 1u ? 1u : 2u;
-                else if (ig != 1 && ig != 2 && ig != 4)
-                    ig = 4;
+                // warp items: 1, 2 or 4 particles (FP64); 1, 2 (a packed
+                // pair) or 4 (two packed pairs) in the mixed form
+                if (ig != 1 && ig != 2 && ig != 4) ig = MODE == H4_FORCE_MIXED ? 2 : 4;
                 chunk = max(32u, (chunk + 31u) & ~31u);
                 split = ((unsigned)n + chunk - 1) / chunk;
                 const unsigned cap = nact ? (unsigned)(S.part_cap / (6ull * nact)) : 1u;
@@ -780,6 +777,88 @@ __device__ bool ring_warp_item(const Dev &d, const System &S, const unsigned *mo
     return true;
 }
 
+// The same for four active particles k0 .. k0 + 3 as two packed pairs: every
+// j a lane loads, and the duplication of its values into register pairs, then
+// serves both pairs, and every stage wait and refill four particles.  To fit
+// the registers, each lane sums its j of the chunk in plain FP32 (chunk / 32
+// terms, no runs or Kahan pairs); the lanes' sums are then added in
+// double-single as the other items do.
+__device__ bool ring_warp_item4(const Dev &d, const System &S, const unsigned *move, unsigned nact, unsigned k0,
+                                int jb, int je, double *part_s, float4 (*ring)[3][WARP_STAGE_J], uint64_t *wfull,
+                                unsigned &gw, int lane) {
+    using namespace pair;
+    const float4 *jf0 = d.jf0 + S.off, *jf1 = d.jf1 + S.off, *jf2 = d.jf2 + S.off;
+    const float e2f = (float)S.e2;
+    const int nst = (je - jb + WARP_STAGE_J - 1) / WARP_STAGE_J;
+    const unsigned gs0 = gw;
+    if (lane == 0)
+        for (int k = 0; k < WARP_STAGES && k < nst; k++)
+            issue_stage(ring, wfull, gs0 + k, jf0, jf1, jf2, jb + k * WARP_STAGE_J,
+                        min(WARP_STAGE_J, je - jb - k * WARP_STAGE_J));
+    const IPair ip0 = pack_pair(load_i(jf0, jf1, jf2, move[k0]), load_i(jf0, jf1, jf2, move[k0 + 1]));
+    const IPair ip1 = pack_pair(load_i(jf0, jf1, jf2, move[k0 + 2]), load_i(jf0, jf1, jf2, move[k0 + 3]));
+    const f2 e2 = pk2(e2f, e2f), m3 = pk2(-3.0f, -3.0f);
+    f2 T0[6], T1[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) { T0[c] = 0ull; T1[c] = 0ull; }
+    bool ok = true;
+    int k = 0;
+    for (; k < nst; k++) {
+        const unsigned gs = gs0 + (unsigned)k, st = gs % WARP_STAGES;
+        ok = __all_sync(0xffffffffu, tma::wait_bounded(&wfull[st], (gs / WARP_STAGES) & 1u, WAIT_LIMIT));
+        if (!ok) break;
+        const int j0 = jb + k * WARP_STAGE_J;
+#pragma unroll
+        for (int h = 0; h < WARP_STAGE_J / 32; h++) {
+            const int jj = lane + 32 * h;
+            if (j0 + jj < je) {
+                const float4 a = ring[st][0][jj], b = ring[st][1][jj], c = ring[st][2][jj];
+                const f2 xh = pk2(a.x, a.x), yh = pk2(a.y, a.y), zh = pk2(a.z, a.z), m = pk2(a.w, a.w);
+                const f2 xl = pk2(b.x, b.x), yl = pk2(b.y, b.y), zl = pk2(b.z, b.z);
+                const f2 vx = pk2(c.x, c.x), vy = pk2(c.y, c.y), vz = pk2(c.z, c.z);
+                pair_x2(ip0, xh, yh, zh, m, xl, yl, zl, vx, vy, vz, e2, m3, T0);
+                pair_x2(ip1, xh, yh, zh, m, xl, yl, zl, vx, vy, vz, e2, m3, T1);
+            }
+        }
+        __syncwarp();
+        if (lane == 0 && k + WARP_STAGES < nst)
+            issue_stage(ring, wfull, gs + WARP_STAGES, jf0, jf1, jf2, j0 + WARP_STAGES * WARP_STAGE_J,
+                        min(WARP_STAGE_J, je - j0 - WARP_STAGES * WARP_STAGE_J));
+    }
+    if (!ok) {
+        if (lane == 0) {   // stages possibly still in flight: k .. k + WARP_STAGES - 1
+            for (int q = k; q < nst && q < k + WARP_STAGES; q++)
+                tma::wait_bounded(&wfull[(gs0 + q) % WARP_STAGES], ((gs0 + q) / WARP_STAGES) & 1u, WAIT_LIMIT);
+            atomicOr(d.err, (unsigned)H4_ERRBIT_TIMEOUT);
+        }
+        return false;
+    }
+    gw = gs0 + (unsigned)nst;
+    // the lanes' totals summed in double-single FP32, three components at a
+    // time: value 4c' + q is component 3 half + c' of particle k0 + q
+    constexpr int V = 16;
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        float h[V], l[V];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const int cc = 3 * half + c;
+            h[4 * c] = lo2(T0[cc]); h[4 * c + 1] = hi2(T0[cc]);
+            h[4 * c + 2] = lo2(T1[cc]); h[4 * c + 3] = hi2(T1[cc]);
+        }
+#pragma unroll
+        for (int x = 0; x < V; x++) {
+            l[x] = 0.f;
+            if (x >= 12) h[x] = 0.f;
+        }
+        rs_sum_ds<V, 16>(h, l, lane);
+        const int x = rs_index<V>(lane);
+        if (rs_first<V>(lane) && x < 12)
+            part_s[(size_t)(3 * half + x / 4) * nact + k0 + (x % 4)] = (double)h[0] + (double)l[0];
+    }
+    return true;
+}
+
 // ---- P1: one warp item of some system's force sum ---------------------------
 template <int MODE>
 __device__ bool force_item(const Dev &d, const System &S, unsigned local, int lane, float4 (*ring)[3][WARP_STAGE_J],
@@ -820,8 +899,16 @@ __device__ bool force_item(const Dev &d, const System &S, unsigned local, int la
         const float4 *a = d.jf0 + off, *b = d.jf1 + off, *c = d.jf2 + off;
         const float e2 = (float)S.e2;
         if (S.e2 > 0.0)   // a packed pair, or one particle, j through the warp's ring
-            return cnt == 2 ? ring_warp_item<2>(d, S, move, nact, k0, jb, je, part_s, ring, wfull, gw, lane)
-                            : ring_warp_item<1>(d, S, move, nact, k0, jb, je, part_s, ring, wfull, gw, lane);
+        {   // four particles (two packed pairs), a packed pair, or one; j through the warp's ring
+            if (cnt == 4) return ring_warp_item4(d, S, move, nact, k0, jb, je, part_s, ring, wfull, gw, lane);
+            unsigned k = k0;
+            if (cnt >= 2) {
+                if (!ring_warp_item<2>(d, S, move, nact, k, jb, je, part_s, ring, wfull, gw, lane)) return false;
+                k += 2;
+            }
+            if (cnt & 1) return ring_warp_item<1>(d, S, move, nact, k, jb, je, part_s, ring, wfull, gw, lane);
+            return true;
+        }
         {   // e2 = 0: the self term masked, j from L2
             unsigned k = k0;
             while (k < k0 + cnt) {
@@ -1429,20 +1516,22 @@ void ens_free(h4_ensemble_s *E) {
 
 // Default tuning table (used until a tuned table is loaded).  FP64: up to 4
 // particles per warp item; j-chunks short for small active sets (more
-// items), the whole system for large ones.  Mixed: warp items of a packed
-// pair below 1024 active particles, block-tiled items of 512 particles above,
+// items), the whole system for large ones.  Mixed: warp items of two packed
+// pairs below 1024 active particles (one pair below 4) against 1024-j chunks
+// (128 for the smallest steps), block-tiled items of 512 particles above,
 // 1024 j per block item (many items per step: in an ensemble few systems
 // take a large step in the same iteration), tiles of 256.
 void default_tuning(int mode, unsigned *ig, unsigned *chunk, unsigned *jt) {
     static const unsigned ch[NB_A] = {128, 128, 256, 512, 1024, 2048, 4096, 8192};
-    static const unsigned mixed_ig[NB_A] = {1, 2, 2, 2, 2, 2, 512, 512};
+    static const unsigned mixed_ig[NB_A] = {1, 2, 4, 4, 4, 4, 512, 512};
+    static const unsigned mixed_ch[NB_A] = {128, 128, 1024, 1024, 1024, 1024, 1024, 1024};
     for (int b = 0; b < NB_N; b++) {
         for (int a = 0; a < NB_A; a++) {
             const int t = b * NB_A + a;
             jt[t] = JT_MAX;
             if (mode == H4_FORCE_MIXED) {
                 ig[t] = mixed_ig[a];
-                chunk[t] = mixed_ig[a] > 2 ? 1024 : ch[a];
+                chunk[t] = mixed_ch[a];
             } else {
                 ig[t] = 4;
                 chunk[t] = ch[a];
@@ -1467,7 +1556,7 @@ size_t part_cap_for(unsigned n, size_t splits) { return 6 * (splits * (size_t)n 
 // Checks a tuning table for the ensemble's force mode (see h4_ens_set_tuning).
 bool tuning_valid(int mode, const unsigned *ig, const unsigned *chunk, const unsigned *jt) {
     for (int t = 0; t < NB_N * NB_A; t++) {
-        const bool warp = ig[t] == 1 || ig[t] == 2 || (ig[t] == 4 && mode != H4_FORCE_MIXED);
+        const bool warp = ig[t] == 1 || ig[t] == 2 || ig[t] == 4;
         const bool block = mode == H4_FORCE_MIXED && ig[t] >= BTI_MIN && ig[t] <= BTI_MAX && (ig[t] & (ig[t] - 1)) == 0;
         if (!(warp || block) || chunk[t] < 32 || chunk[t] > (1u << 24)) return false;
         if (jt && jt[t] != 128 && jt[t] != 256) return false;
@@ -1653,7 +1742,7 @@ int h4_ens_set_tuning(h4_ens_handle E, const unsigned int *ig, const unsigned in
     if (!E || !ig || !chunk) return efail(H4_ERR_ARG, "h4_ens_set_tuning: null argument");
     if (!tuning_valid(E->mode, ig, chunk, jtile))
         return efail(H4_ERR_ARG, E->mode == H4_FORCE_MIXED
-                                     ? "h4_ens_set_tuning: ig must be 1 or 2 (warp items) or a power of two in "
+                                     ? "h4_ens_set_tuning: ig must be 1, 2 or 4 (warp items) or a power of two in "
                                        "[16, 512] (block items), chunk in [32, 2^24], jtile 128 or 256"
                                      : "h4_ens_set_tuning: ig must be 1, 2 or 4 and chunk in [32, 2^24]");
     std::vector<unsigned> jt(NB_N * NB_A, (unsigned)JT_MAX);

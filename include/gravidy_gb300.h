@@ -197,9 +197,10 @@ typedef struct h4_ensemble_s *h4_ens_handle;
  * <=1k, <=2k, <=4k, <=8k, larger; active buckets: 1, 2-3, 4-15, 16-63,
  * 64-255, 256-1023, 1024-4095, >=4096.
  *   ig     FP64 and exact forms: particles per warp item (1, 2 or 4).
- *          Mixed form: 1 or 2 = warp items (lanes over j; 2 = one packed
- *          pair), or a power of two in [16, 512] = block-tiled items of ig
- *          particles (lanes over i, j tiles in shared memory).
+ *          Mixed form: 1, 2 or 4 = warp items (lanes over j; 2 = one
+ *          packed pair, 4 = two), or a power of two in [16, 512] =
+ *          block-tiled items of ig particles (lanes over i, j tiles in
+ *          shared memory).
  *   chunk  j per item (rounded up to whole tiles for block items).
  *   jtile  j per shared-memory tile of a block item, 128 or 256 (NULL: 256). */
 #define H4_ENS_TUNE_NB_N 6

@@ -120,7 +120,7 @@ def test_header_constants_match_the_binding():
 def test_committed_tuning_table_is_well_formed():
     """gravidy_gb300/tuning/ensemble_gb300.json: one table per force form
     covering every (N, N_act) bucket (NB_N x NB_A entries).  FP64: ig in
-    {1, 2, 4}, chunks multiples of 32.  Mixed: ig 1 or 2 (warp items) or a
+    {1, 2, 4}, chunks multiples of 32.  Mixed: ig 1, 2 or 4 (warp items) or a
     power of two in [16, 512] (block-tiled items), j tiles of 128 or 256 and
     block-item chunks a whole number of tiles; the mixture weights the tuner
     recorded have the same shape."""
@@ -139,7 +139,7 @@ def test_committed_tuning_table_is_well_formed():
             assert set(np.unique(ig)) <= {1, 2, 4}
         else:
             assert "jtile" in T
-            assert set(np.unique(ig)) <= {1, 2, 16, 32, 64, 128, 256, 512}
+            assert set(np.unique(ig)) <= {1, 2, 4, 16, 32, 64, 128, 256, 512}
             assert set(np.unique(jt)) <= {128, 256}
             block = ig >= 16
             assert np.all(ch[block] % jt[block] == 0)
