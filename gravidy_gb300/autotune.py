@@ -84,6 +84,15 @@ def mixed_candidates(n: int, a: int):
     return [c for c in out if c[1] <= 2 * n]
 
 
+def pick_within_tie(times, tie: float = TIE) -> int:
+    """Index of the first candidate whose time is within `tie` of the
+    fastest: the descent lists the current choice first, so a candidate must
+    beat it by more than the tie band to replace it, and among near-equals
+    the earlier one wins -- the same times always give the same pick."""
+    best = min(times)
+    return next(i for i, t in enumerate(times) if t <= best * (1.0 + tie))
+
+
 def record_mixture(mode: str, t_end: float = 0.25, verbose: bool = True):
     """Block steps and interactions per bucket of the C4 ensemble run to
     t_end with the default table."""
@@ -150,7 +159,7 @@ def tune_descent(mode: str, verbose: bool = True) -> dict:
             trial["ig"][b][a], trial["chunk"][b][a], trial["jtile"][b][a] = c
             times.append(c4_seconds(mode, systems, trial, t_eval))
         best = min(times)
-        pick = next(i for i, t in enumerate(times) if t <= best * (1.0 + TIE))
+        pick = pick_within_tie(times)
         table["ig"][b][a], table["chunk"][b][a], table["jtile"][b][a] = cands[pick]
         t_best = times[pick]
         trace.append({"bucket": [b, a], "weight": float(w), "candidates": [list(c) for c in cands],

@@ -167,6 +167,22 @@ def test_autotuner_candidates_are_valid_table_entries():
                         assert mode == "mixed" and chunk % jt == 0
 
 
+def test_autotuner_pick_rule():
+    """The descent's pick: the current choice (listed first) stays unless a
+    candidate beats it by more than the tie band; among candidates within
+    the band of the fastest the earliest wins."""
+    from gravidy_gb300.autotune import TIE, pick_within_tie
+    assert pick_within_tie([1.0, 0.995, 0.999]) == 0            # within 1 %: keep the current
+    assert pick_within_tie([1.0, 0.98, 0.985]) == 1             # beaten by 2 %: the first near-best
+    assert pick_within_tie([1.0, 0.985, 0.98]) == 1             # 0.985 is within 1 % of 0.98
+    assert pick_within_tie([1.0, 0.97, 0.95]) == 2
+    assert pick_within_tie([1.0, 0.97, 0.95], tie=0.05) == 1   # 0.97 <= 0.95 * 1.05
+    assert pick_within_tie([1.0, 0.97, 0.95], tie=0.06) == 0   # 1.0 <= 0.95 * 1.06
+    times = [0.7791, 0.7817, 0.8027, 0.7660, 0.7718]
+    assert pick_within_tie(times) == pick_within_tie(list(times)) == 3   # repeatable
+    assert TIE == 0.01
+
+
 def test_c4_sizes_are_seeded_and_in_range():
     from gravidy_gb300 import workloads
     a = workloads.c4_sizes(256, seed=7)
